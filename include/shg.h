@@ -1,0 +1,116 @@
+/* shg_gb300 — C ABI of the GB300 SSFM z-march for focused-Gaussian-beam SHG.
+ *
+ * Drop-in boundary for the reference's solver path (alfredos84/SHG_Focused_Gaussian_Beams,
+ * src/headers/Solver.h and the setup classes it drives). Every entry point returns an
+ * int status (SHG_OK = 0); shg_last_error() gives the message of the last failure on the
+ * calling thread. Plain pointers and sizes only. Complex fields are interleaved float
+ * re/im in the reference layout IDX(x, y) = y*NX + x (Common.h:27-29); temperature
+ * tensors are float IDX(x, y, z) = z*NX*NY + y*NX + x. Lengths in um, temperatures in C,
+ * powers in W (Crystal.h:19-21).
+ */
+#ifndef SHG_GB300_H
+#define SHG_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SHG_OK 0
+#define SHG_ERR_INVALID 1      /* bad argument or configuration */
+#define SHG_ERR_UNSUPPORTED 2  /* valid for the reference, not implemented on the device */
+#define SHG_ERR_CUDA 3         /* CUDA runtime error */
+#define SHG_ERR_NOMEM 4        /* device or host allocation failed */
+#define SHG_ERR_STATE 5        /* call order (e.g. fields requested before a run) */
+#define SHG_ERR_NONFINITE 6    /* a result is NaN or infinite */
+
+/* Grid, crystal and run options. Replaces the compile-time constants of SHG.cpp:11-20
+ * and Crystal.h:26-53 and the -DTHERMAL switch (SHG.sh:20-23). */
+typedef struct shg_config {
+    int nx, ny, nz;          /* SHG.cpp:11-13 */
+    float lx, ly, lz;        /* Crystal.h:31-33: window width, height, crystal length */
+    float lp;                /* Crystal.h:26: pump wavelength (SH at lp/2) */
+    float deff;              /* Crystal.h:41 (dQ = 2/pi * deff, Crystal.h:42) */
+    float lambda_qpm;        /* Crystal.h:43: poling period */
+    float alpha_p, alpha_s;  /* Crystal.h:44-45: linear absorption, 1/um */
+    float beta_s;            /* Crystal.h:46: SH two-photon absorption, um/W */
+    float rho_p, rho_s;      /* Crystal.h:47-48: walk-off angles, rad */
+    float kth, htc;          /* Crystal.h:52-53: thermal conductivity, heat-transfer coefficient */
+    int thermal;             /* 1 = the -DTHERMAL build (Solver.h:289-340) */
+    int bc;                  /* 0 = open top, bottom ovens (Tfield.h:113); 1 = oven surrounded (Tfield.h:224) */
+    int sh_seed;             /* < 0: SH starts at zero; >= 0: seeded N(0, 1e-20) (Efields.h:129-144) */
+    int device;              /* CUDA device ordinal */
+} shg_config;
+
+/* Fills `cfg` with the reference's compiled-in values (64x64x200 grid, 2000x1000x30000 um
+ * MgO:sPPLT crystal, Crystal.h:26-53), thermal off, open-top BC, zero SH start, device 0. */
+int shg_config_init(shg_config *cfg);
+
+typedef struct shg_handle shg_handle;
+
+/* Allocates the device state of one solve (the Efields/Tfield/PhaseMatching/Solver
+ * objects of Solver.h:283-285 and 126-146). Grids must be square with NX = NY a power of
+ * two in [16, 256]; other grids return SHG_ERR_UNSUPPORTED. */
+int shg_create(const shg_config *cfg, shg_handle **out);
+int shg_destroy(shg_handle *h);
+
+/* Solver::run (Solver.h:279-355), same arguments in the same order. The output fields are
+ * the state at the top of slice NZ-1 (what Solver::CWES saves as Pump_out/Signal_out,
+ * Solver.h:250-255) and stay on the device until read. save_only_last / save_temperature
+ * select the reference's text outputs when an output directory is set
+ * (shg_set_output_dir); otherwise they are ignored. */
+int shg_run(shg_handle *h, float power, float waist, float focalpoint, float temp, float t_inf,
+            float t_peltier1, float t_peltier2, int save_only_last, int save_temperature);
+
+/* Efields::setInputPump (Efields.h:174 -> setPump, Efields.h:74): Gaussian pump with the
+ * refractive index taken at temperature tc. */
+int shg_set_input_pump(shg_handle *h, float power, float focalpoint, float waist, float tc);
+/* Arbitrary input fields (host, NX*NY complex each); sh may be NULL for a zero start. */
+int shg_set_input_fields(shg_handle *h, const float *pump, const float *sh);
+/* Solver::CWES (Solver.h:245) without THERMAL from the current input fields, with the
+ * propagators (Efields.h:186) and the constant phase mismatch (PhaseMatching.h:113)
+ * set at temperature `temp`. */
+int shg_cwes(shg_handle *h, float temp);
+/* Same, with device pointers (NX*NY complex64 each) and a cudaStream_t (NULL = default). */
+int shg_cwes_device(shg_handle *h, float temp, const void *pump_in, const void *sh_in, void *pump_out,
+                    void *sh_out, void *stream);
+
+/* Results of the last run. Fields: host buffers of NX*NY complex (interleaved float). */
+int shg_get_fields(shg_handle *h, float *pump_out, float *sh_out);
+/* P = 1/2 eps0 c n sum|A|^2 dx dy with n the pump / SH index at the run temperature. */
+int shg_get_powers(shg_handle *h, double *p_pump_in, double *p_sh_out, double *p_pump_out);
+int shg_efficiency(shg_handle *h, double *eta);
+
+const char *shg_last_error(void);
+
+/* ---- Batched sweep: many independent plain solves in one device schedule ----------- */
+typedef struct shg_instance {
+    int nx, ny, nz;          /* per-solve grid (square, power of two) */
+    float lx, ly;            /* per-solve window */
+    float power, waist, temp, focal;  /* Solver::run arguments (Temp also sets delta-k) */
+} shg_instance;
+
+typedef struct shg_batch shg_batch;
+/* `crystal` supplies lz, lp, deff, lambda_qpm, absorption and walk-off; its grid and
+ * window fields are ignored. */
+int shg_batch_create(const shg_config *crystal, const shg_instance *inst, int n, shg_batch **out);
+int shg_batch_destroy(shg_batch *b);
+/* Runs every solve and copies the efficiencies (n doubles) to the host; when fields_out
+ * is not NULL, fields_out[i] receives the SH output field of solve i (NX*NY complex). */
+int shg_batch_run(shg_batch *b, double *eta, float **fields_out);
+/* Device-only run on `stream` (results stay on the device); shg_batch_results copies the
+ * efficiencies after the stream has been synchronised. */
+int shg_batch_run_async(shg_batch *b, void *stream);
+int shg_batch_results(shg_batch *b, double *eta);
+/* Number of kernel launches one run issues. */
+int shg_batch_launch_count(shg_batch *b, int *launches);
+
+/* ---- Components, for tests ------------------------------------------------------- */
+/* Unnormalised 2D DFT of an n x n complex array on the device (sign -1 forward, +1
+ * backward, FFTW's convention), device pointers, in place allowed. */
+int shg_dft2d_device(int n, int sign, const void *in, void *out, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

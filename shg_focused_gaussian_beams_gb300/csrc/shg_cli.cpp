@@ -1,0 +1,119 @@
+// `shg` command line: the argument list of the reference's SHG binary
+// (src/SHG.cpp:37-50, driven by src/SHG.sh:81):
+//
+//     shg <P [W]> <waist [um]> <T1 [C], also Temp> <T2 [C]> <SOLS 0/1> <STMP 0/1> [options]
+//
+// The grid and crystal, compile-time constants in the reference (SHG.cpp:11-13,
+// Crystal.h:26-53), are options here: --nx N --ny N --nz N --lx um --ly um --lz um
+// --deff um/V --lambda um --alpha-p 1/um --alpha-s 1/um --beta-s um/W --thermal --bc 0|1
+// --outdir DIR --device K. Output files follow Files.h:36-57 (Pump_out_r.dat, ...).
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iomanip>
+#include <iostream>
+#include <string>
+#include <vector>
+
+#include "../../include/shg.h"
+
+namespace {
+
+// Files.h:36-57: tab-separated, 20 significant digits, one row per y.
+void save_matrix_complex(const std::string &dir, const std::string &name, const std::vector<float> &v, int nx,
+                         int ny) {
+    for (int part = 0; part < 2; ++part) {
+        std::ofstream f(dir + "/" + name + (part == 0 ? "_r.dat" : "_i.dat"));
+        for (int iy = 0; iy < ny; ++iy) {
+            for (int ix = 0; ix < nx; ++ix) f << std::setprecision(20) << v[2 * ((size_t)iy * nx + ix) + part] << "\t";
+            f << "\n";
+        }
+    }
+}
+
+int fail(const char *what, int rc) {
+    std::cerr << what << " failed (" << rc << "): " << shg_last_error() << std::endl;
+    return 1;
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+    std::cout << "#######---SHG efficiency calculator (GB300)---#######\n\n" << std::endl;
+    if (argc < 7) {
+        std::cerr << "usage: shg P waist T1 T2 SOLS STMP [--nx N --ny N --nz N --lx um --ly um --lz um "
+                     "--deff um/V --lambda um --alpha-p v --alpha-s v --beta-s v --thermal --bc 0|1 "
+                     "--outdir DIR --device K]"
+                  << std::endl;
+        return 2;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    shg_config cfg;
+    shg_config_init(&cfg);
+    std::string outdir = ".";
+    for (int i = 7; i < argc; ++i) {
+        const std::string a = argv[i];
+        auto val = [&]() -> const char * {
+            if (i + 1 >= argc) {
+                std::cerr << "missing value for " << a << std::endl;
+                std::exit(2);
+            }
+            return argv[++i];
+        };
+        if (a == "--nx") cfg.nx = std::atoi(val());
+        else if (a == "--ny") cfg.ny = std::atoi(val());
+        else if (a == "--nz") cfg.nz = std::atoi(val());
+        else if (a == "--lx") cfg.lx = (float)std::atof(val());
+        else if (a == "--ly") cfg.ly = (float)std::atof(val());
+        else if (a == "--lz") cfg.lz = (float)std::atof(val());
+        else if (a == "--deff") cfg.deff = (float)std::atof(val());
+        else if (a == "--lambda") cfg.lambda_qpm = (float)std::atof(val());
+        else if (a == "--alpha-p") cfg.alpha_p = (float)std::atof(val());
+        else if (a == "--alpha-s") cfg.alpha_s = (float)std::atof(val());
+        else if (a == "--beta-s") cfg.beta_s = (float)std::atof(val());
+        else if (a == "--thermal") cfg.thermal = 1;
+        else if (a == "--bc") cfg.bc = std::atoi(val());
+        else if (a == "--outdir") outdir = val();
+        else if (a == "--device") cfg.device = std::atoi(val());
+        else {
+            std::cerr << "unknown option " << a << std::endl;
+            return 2;
+        }
+    }
+    // SHG.cpp:37-50
+    const float Power = (float)std::atof(argv[1]);
+    const float waist = (float)std::atof(argv[2]);
+    const float focalpoint = (float)(0.5 * cfg.lz);
+    const float Temp = (float)std::atof(argv[3]);
+    const float T_inf = 25;
+    const float Tpeltier1 = (float)std::atof(argv[3]);
+    const float Tpeltier2 = (float)std::atof(argv[4]);
+    const bool save_only_last = std::atoi(argv[5]);
+    const bool save_temperature = std::atoi(argv[6]);
+    std::cout << "\n\nPump power =  " << Power << " W" << std::endl;
+    std::cout << "Beam waist = " << waist << " μm" << std::endl;
+    std::cout << "Focal distance = " << focalpoint << " μm" << std::endl;
+    std::cout << "Phase-matching temperature =  " << Temp << " ºC" << std::endl;
+    std::cout << "Environment temperature =  " << T_inf << " ºC" << std::endl;
+    std::cout << "Peltier 1 temperature =  " << Tpeltier1 << " ºC" << std::endl;
+    std::cout << "Peltier 2 temperature =  " << Tpeltier2 << " ºC\n" << std::endl;
+
+    shg_handle *h = nullptr;
+    int rc = shg_create(&cfg, &h);
+    if (rc) return fail("shg_create", rc);
+    rc = shg_run(h, Power, waist, focalpoint, Temp, T_inf, Tpeltier1, Tpeltier2, save_only_last, save_temperature);
+    if (rc) return fail("shg_run", rc);
+    std::vector<float> pump((size_t)2 * cfg.nx * cfg.ny), sh(pump.size());
+    rc = shg_get_fields(h, pump.data(), sh.data());
+    if (rc) return fail("shg_get_fields", rc);
+    save_matrix_complex(outdir, "Pump_out", pump, cfg.nx, cfg.ny);
+    save_matrix_complex(outdir, "Signal_out", sh, cfg.nx, cfg.ny);
+    double eta = 0;
+    if (shg_efficiency(h, &eta) == SHG_OK) std::cout << "Conversion efficiency = " << std::setprecision(9) << eta << std::endl;
+    shg_destroy(h);
+    const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    std::cout << "\n\n...time elapsed " << el << " seconds\n\n " << std::endl;
+    return 0;
+}

@@ -1,0 +1,204 @@
+// Line FFTs for the transverse diffraction step (replaces the fftwf_plan_dft_2d /
+// fftwf_execute calls of Solver.h:161-187).
+//
+// A line of N complex points is held by a group of G threads, E = N/G points per thread,
+// and transformed in two register stages with one shared-memory transpose between them
+// (N = E * G, x = t + G*j on input):
+//
+//   stage 1: each thread runs an E-point DFT over its registers (compile-time twiddles),
+//   twiddle:  multiply by w_N^(t*k2) from a table evaluated in double and rounded once,
+//   transpose through shared memory,
+//   stage 2: each thread runs E/G DFTs of G points.
+//
+// Two register layouts matter to callers:
+//   natural  L_in : thread t, register j          <-> index t + G*j
+//   spectral L_out: thread t, register m*G + k1   <-> index (t*(E/G) + m) + E*k1
+// `fft_nat_to_spec` maps L_in data to its DFT in L_out; `fft_spec_to_nat` maps L_out
+// data to its DFT in L_in (the transposed factorisation of the same symmetric DFT
+// matrix). Pointwise work between a transform and the next one in the other direction
+// (propagator products, the RK4 coupling) therefore never reorders data.
+//
+// SIGN = -1 is FFTW_FORWARD (exp(-2 pi i jk/N)), SIGN = +1 is FFTW_BACKWARD.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <utility>
+
+namespace shg {
+
+__device__ __forceinline__ float2 c_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 c_sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 c_mul(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+// a * conj(b)
+__device__ __forceinline__ float2 c_mulc(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
+}
+
+template <int... Is, class F>
+__device__ __forceinline__ void sfor_impl(std::integer_sequence<int, Is...>, F &&f) {
+    (f(std::integral_constant<int, Is>{}), ...);
+}
+// Compile-time unrolled loop: f(std::integral_constant<int, i>) for i in [0, N).
+template <int N, class F>
+__device__ __forceinline__ void sfor(F &&f) {
+    sfor_impl(std::make_integer_sequence<int, N>{}, f);
+}
+
+__host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n / 2); }
+__host__ __device__ constexpr int bitrev(int i, int bits) {
+    int r = 0;
+    for (int b = 0; b < bits; ++b)
+        if (i & (1 << b)) r |= 1 << (bits - 1 - b);
+    return r;
+}
+
+// cos / sin of 2*pi*m/32, m < 16, evaluated in double and rounded to float.
+struct W32 {
+    static constexpr float c[16] = {1.0f, 0.9807852506637573f, 0.9238795042037964f, 0.8314695954322815f,
+                                    0.7071067690849304f, 0.5555702447891235f, 0.3826834261417389f,
+                                    0.19509032368659973f, 0.0f, -0.19509032368659973f, -0.3826834261417389f,
+                                    -0.5555702447891235f, -0.7071067690849304f, -0.8314695954322815f,
+                                    -0.9238795042037964f, -0.9807852506637573f};
+    static constexpr float s[16] = {0.0f, 0.19509032368659973f, 0.3826834261417389f, 0.5555702447891235f,
+                                    0.7071067690849304f, 0.8314695954322815f, 0.9238795042037964f,
+                                    0.9807852506637573f, 1.0f, 0.9807852506637573f, 0.9238795042037964f,
+                                    0.8314695954322815f, 0.7071067690849304f, 0.5555702447891235f,
+                                    0.3826834261417389f, 0.19509032368659973f};
+};
+
+// b * exp(SIGN * 2 pi i M / 32), with the exact special cases M = 0, 4, 8, 12.
+template <int SIGN, int M>
+__device__ __forceinline__ float2 tw_const(float2 b) {
+    constexpr float r = 0.7071067690849304f;
+    if constexpr (M == 0) {
+        return b;
+    } else if constexpr (M == 8) {
+        return SIGN > 0 ? make_float2(-b.y, b.x) : make_float2(b.y, -b.x);
+    } else if constexpr (M == 4) {
+        return SIGN > 0 ? make_float2((b.x - b.y) * r, (b.y + b.x) * r)
+                        : make_float2((b.x + b.y) * r, (b.y - b.x) * r);
+    } else if constexpr (M == 12) {
+        return SIGN > 0 ? make_float2(-(b.x + b.y) * r, (b.x - b.y) * r)
+                        : make_float2((b.y - b.x) * r, -(b.x + b.y) * r);
+    } else {
+        constexpr float c = W32::c[M];
+        constexpr float s = SIGN > 0 ? W32::s[M] : -W32::s[M];
+        return make_float2(fmaf(b.x, c, -b.y * s), fmaf(b.x, s, b.y * c));
+    }
+}
+
+// In-register DFT of E <= 32 points held in v[OFF .. OFF+E), natural order in and out
+// (radix-2 decimation in time over a bit-reversed copy; the permutations are renamings).
+template <int E, int SIGN, int OFF = 0, int NV>
+__device__ __forceinline__ void dft_reg(float2 (&v)[NV]) {
+    static_assert(E >= 1 && E <= 32 && (E & (E - 1)) == 0, "register DFT size");
+    if constexpr (E == 1) return;
+    constexpr int LG = ilog2(E);
+    float2 t[E];
+    sfor<E>([&](auto I) { t[bitrev(decltype(I)::value, LG)] = v[OFF + decltype(I)::value]; });
+    sfor<LG>([&](auto S) {
+        constexpr int len = 2 << decltype(S)::value;
+        constexpr int half = len / 2;
+        sfor<E / 2>([&](auto B) {
+            constexpr int grp = decltype(B)::value / half, k = decltype(B)::value % half;
+            constexpr int a = grp * len + k, b = a + half;
+            const float2 y = tw_const<SIGN, k * (32 / len)>(t[b]);
+            const float2 x = t[a];
+            t[a] = c_add(x, y);
+            t[b] = c_sub(x, y);
+        });
+    });
+    sfor<E>([&](auto I) { v[OFF + decltype(I)::value] = t[decltype(I)::value]; });
+}
+
+// Twiddle w_N^m for direction SIGN from a table tab[m] = exp(-2 pi i m / N).
+template <int SIGN>
+__device__ __forceinline__ float2 tw_table(const float2 *__restrict__ tab, int m) {
+    const float2 w = __ldg(tab + m);
+    return SIGN > 0 ? make_float2(w.x, -w.y) : w;
+}
+
+// Per-line shared scratch: E rows of G entries padded to G+1, plus a line pad.
+__host__ __device__ constexpr int pad_to_8_mod_16(int s) {
+    while (s % 16 != 8) ++s;
+    return s;
+}
+template <int N, int G>
+struct LineScratch {
+    static constexpr int E = N / G;
+    static constexpr int GP = G + 1;
+    static constexpr int SIZE = pad_to_8_mod_16(E * GP);
+};
+
+// Lines whose G threads sit in one warp synchronise the warp; lines spread over warps
+// (BS = true) synchronise the block.
+template <bool BS>
+__device__ __forceinline__ void group_sync() {
+    if constexpr (BS) __syncthreads();
+    else __syncwarp();
+}
+
+// Shared-scratch geometry of one line: element (row e < E, column g < G) lives at
+// sc[(e * GP + g) * STRIDE]. Lines held by consecutive lanes (FAST passes) use STRIDE = 1,
+// GP = G + 1 and a padded per-line base; lines interleaved across lanes (column passes)
+// use STRIDE = lines per block, GP = G and base = scratch + line.
+// L_in -> DFT in L_out.
+template <int N, int G, int SIGN, bool BS = false, int STRIDE = 1, int GP = G + 1>
+__device__ __forceinline__ void fft_nat_to_spec(float2 (&v)[N / G], int t, float2 *sc, const float2 *__restrict__ tab) {
+    constexpr int E = N / G, Q = E / G;
+    static_assert(E % G == 0, "need G <= E with G | E");
+    dft_reg<E, SIGN>(v);
+#pragma unroll
+    for (int k2 = 1; k2 < E; ++k2) v[k2] = c_mul(v[k2], tw_table<SIGN>(tab, (t * k2) & (N - 1)));
+    group_sync<BS>();
+#pragma unroll
+    for (int k2 = 0; k2 < E; ++k2) sc[(k2 * GP + t) * STRIDE] = v[k2];
+    group_sync<BS>();
+#pragma unroll
+    for (int m = 0; m < Q; ++m)
+#pragma unroll
+        for (int tt = 0; tt < G; ++tt) v[m * G + tt] = sc[((t * Q + m) * GP + tt) * STRIDE];
+    sfor<Q>([&](auto M) { dft_reg<G, SIGN, decltype(M)::value * G>(v); });
+}
+
+// L_out -> DFT in L_in.
+template <int N, int G, int SIGN, bool BS = false, int STRIDE = 1, int GP = G + 1>
+__device__ __forceinline__ void fft_spec_to_nat(float2 (&v)[N / G], int t, float2 *sc, const float2 *__restrict__ tab) {
+    constexpr int E = N / G, Q = E / G;
+    static_assert(E % G == 0, "need G <= E with G | E");
+    sfor<Q>([&](auto M) { dft_reg<G, SIGN, decltype(M)::value * G>(v); });
+    group_sync<BS>();
+#pragma unroll
+    for (int m = 0; m < Q; ++m)
+#pragma unroll
+        for (int tt = 0; tt < G; ++tt) sc[((t * Q + m) * GP + tt) * STRIDE] = v[m * G + tt];
+    group_sync<BS>();
+#pragma unroll
+    for (int k2 = 0; k2 < E; ++k2) v[k2] = sc[(k2 * GP + t) * STRIDE];
+#pragma unroll
+    for (int k2 = 1; k2 < E; ++k2) v[k2] = c_mul(v[k2], tw_table<SIGN>(tab, (t * k2) & (N - 1)));
+    dft_reg<E, SIGN>(v);
+}
+
+// Index of register r of thread t in the spectral layout L_out.
+template <int N, int G>
+__device__ __forceinline__ int spec_index(int t, int r) {
+    constexpr int E = N / G, Q = E / G;
+    const int m = r / G, k1 = r % G;
+    return (t * Q + m) + E * k1;
+}
+
+// Threads per line for each supported line length (E = N/G points per thread).
+template <int N>
+struct LineShape;
+template <> struct LineShape<16> { static constexpr int G = 4; };
+template <> struct LineShape<32> { static constexpr int G = 4; };
+template <> struct LineShape<64> { static constexpr int G = 8; };
+template <> struct LineShape<128> { static constexpr int G = 8; };
+template <> struct LineShape<256> { static constexpr int G = 16; };
+template <> struct LineShape<512> { static constexpr int G = 16; };
+
+}  // namespace shg

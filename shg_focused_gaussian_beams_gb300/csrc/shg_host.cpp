@@ -1,0 +1,811 @@
+// Host side of the GB300 z-march: crystal set-up with the reference's float semantics,
+// device memory layout, the batched launch schedule (captured in a CUDA graph), and the
+// C ABI declared in include/shg.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "../../include/shg.h"
+#include "shg_internal.h"
+#include "shg_march.cuh"
+
+namespace shg {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+
+#define SHG_CUDA(call)                                                                                 \
+    do {                                                                                               \
+        cudaError_t e_ = (call);                                                                       \
+        if (e_ != cudaSuccess) {                                                                       \
+            set_error(std::string(#call) + ": " + cudaGetErrorString(e_));                            \
+            return e_ == cudaErrorMemoryAllocation ? SHG_ERR_NOMEM : SHG_ERR_CUDA;                     \
+        }                                                                                              \
+    } while (0)
+
+// ---------------------------------------------------------------------------------------
+// Crystal set-up. Every expression keeps the reference's operand order and its implicit
+// float/double promotions; this file is compiled with -ffp-contract=off.
+
+// Crystal.h:80-82
+struct Phys {
+    float PI = (float)3.14159265358979323846;
+    float C = (float)(299792458 * 1E6 / 1E12);
+    float EPS0 = (float)(8.8541878128E-12 * 1E12 / 1E6);
+};
+
+// Crystal.h:116-132: float coefficients, double pow/sqrt, float result.
+float sellmeier(float L, float T) {
+    const float A = 4.502483f, B = 0.007294f, C = 0.185087f, D = -0.02357f;
+    const float E = 0.073423f, F = 0.199595f, G = 0.001f, H = 7.99724f;
+    const double tk = (double)T + 273.15;
+    const float b = (float)(3.483933e-8 * (tk * tk));
+    const float c = (float)(1.607839e-8 * (tk * tk));
+    const double L2 = (double)L * (double)L;
+    const float Cc = C + c, Bb = B + b;
+    const double n2 = (double)A + (double)Bb / (L2 - (double)Cc * (double)Cc) +
+                      (double)E / (L2 - (double)F * (double)F) + (double)G / (L2 - (double)H * (double)H) +
+                      (double)D * L2;
+    return (float)std::sqrt(n2);
+}
+
+struct SolveParams {
+    int n, nz;
+    float lx, ly;
+    float power, waist, focal;
+    float temp;   // coupling and phase-mismatch temperature (dAdz, initDKConstant)
+    float tpump;  // index temperature of the Gaussian pump (setPump reads T at the grid centre)
+    float tprop;  // index temperature of the propagators (beamPropagator, same centre value)
+};
+
+// Fill the scalar part of a descriptor (pointers are set by the caller).
+void fill_scalars(const shg_config &cr, const SolveParams &sp, InstDesc &d) {
+    const Phys ph;
+    const float PI = ph.PI;
+    const int n = sp.n;
+    const float lp = cr.lp, ls = (float)(0.5 * (double)lp);
+    const float dx = sp.lx / (float)(unsigned)(n - 1);
+    const float dy = sp.ly / (float)(unsigned)(n - 1);
+    const float dz = cr.lz / (float)(unsigned)(sp.nz - 1);
+    const float dQ = (float)((2.0 / (double)PI) * (double)cr.deff);
+    d.n = n;
+    d.nz = sp.nz;
+    d.nsteps = sp.nz - 1;
+    d.dz = dz;
+    d.dz6 = dz / 6.0f;
+    // Solver.h:75-77: i*pi*dQ/(n_p*lp), i*0.5*pi*dQ/(n_s*ls); TPA and absorption terms.
+    const float np_t = sellmeier(lp, sp.temp), ns_t = sellmeier(ls, sp.temp);
+    d.kp = (dQ * PI) / (np_t * lp);
+    d.ks = (dQ * (PI * 0.5f)) / (ns_t * ls);
+    d.hp = (float)(0.5 * (double)cr.alpha_p);
+    d.tpa0 = (float)(0.5 * (double)cr.alpha_s);
+    d.tpa1 = (float)(0.5 * ((double)cr.beta_s * 0.5 * (double)ph.C * (double)ph.EPS0 * (double)ns_t));
+    // PhaseMatching.h:57-70
+    d.dk = 2.0f * PI * (2.0f * np_t / lp - ns_t / ls + 1.0f / cr.lambda_qpm);
+    // Efields.h:74-104 at tpump
+    const float np_c = sellmeier(lp, sp.tpump);
+    d.uX = (float)(0.5 * n);
+    d.uY = (float)(0.5 * n);
+    d.dx = dx;
+    d.dy = dy;
+    const float wX2 = sp.waist * sp.waist;
+    const float zRX = PI * np_c * wX2 / lp;
+    const float Ap0 = sqrtf(4.0f * sp.power / (ph.EPS0 * ph.C * PI * np_c * wX2));
+    const float etaX = sp.focal / zRX;
+    const float mre = 1.0f - etaX * 0.0f, mim = -(etaX * 1.0f);
+    const float mden = mre * mre + mim * mim;
+    d.amp = make_float2((+Ap0 * mre) / mden, (-Ap0 * mim) / mden);
+    d.wM = make_float2(wX2 * mre, wX2 * mim);
+    d.wM_den = d.wM.x * d.wM.x + d.wM.y * d.wM.y;
+    // Efields.h:107-126 at tprop
+    const float np_h = sellmeier(lp, sp.tprop), ns_h = sellmeier(ls, sp.tprop);
+    const float kpw = 2.0f * PI * np_h / lp, ksw = 2.0f * PI * ns_h / ls;
+    const float dfX = 1.0f / dx / (float)(unsigned)n, dfY = 1.0f / dy / (float)(unsigned)n;
+    const float pi2 = PI * PI;
+    d.gp = 2.0f * pi2 / kpw;
+    d.gs = 2.0f * pi2 / ksw;
+    d.dfX2 = dfX * dfX;
+    d.dfY2 = dfY * dfY;
+    d.linp = 2.0f * PI * dfX * tanf(cr.rho_p);
+    d.lins = 2.0f * PI * dfX * tanf(cr.rho_s);
+    d.mdz = -dz;
+    d.inv_nn = 1.0f / (float)(n * n);
+}
+
+// Power of a field in W from sum |A|^2 (the efficiency definition used by the tests).
+double field_power(double sum_abs2, float n_index, float dx, float dy) {
+    const Phys ph;
+    return 0.5 * (double)ph.EPS0 * (double)ph.C * (double)n_index * sum_abs2 * (double)dx * (double)dy;
+}
+
+// Twiddle tables exp(-2 pi i m/N), N = 16..256, at [N, 2N) of the device symbol.
+int ensure_twiddles(int device) {
+    static std::mutex mu;
+    static std::map<int, bool> done;
+    std::lock_guard<std::mutex> lock(mu);
+    if (done[device]) return SHG_OK;
+    std::vector<float2> tab(2 * kMaxLine, make_float2(0.f, 0.f));
+    for (int N = 16; N <= kMaxLine; N *= 2)
+        for (int m = 0; m < N; ++m) {
+            const double a = 2.0 * 3.14159265358979323846264338327950288 * (double)m / (double)N;
+            tab[N + m] = make_float2((float)std::cos(a), (float)(-std::sin(a)));
+        }
+    void *p = const_cast<float2 *>(twiddle_symbol_address());
+    if (!p) {
+        set_error("twiddle table symbol unavailable");
+        return SHG_ERR_CUDA;
+    }
+    SHG_CUDA(cudaMemcpy(p, tab.data(), tab.size() * sizeof(float2), cudaMemcpyHostToDevice));
+    done[device] = true;
+    return SHG_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// A set of plain solves with their device buffers and launch schedule.
+class Batch {
+   public:
+    ~Batch() { release(); }
+
+    int create(const shg_config &crystal, const std::vector<SolveParams> &sp) {
+        release();
+        cr_ = crystal;
+        sp_ = sp;
+        const int n = (int)sp.size();
+        if (n <= 0) {
+            set_error("empty batch");
+            return SHG_ERR_INVALID;
+        }
+        for (const auto &s : sp) {
+            if (!line_length_supported(s.n)) {
+                set_error("grid " + std::to_string(s.n) + " not supported (square power of two in [16, 256])");
+                return SHG_ERR_UNSUPPORTED;
+            }
+            if (s.nz < 2) {
+                set_error("nz must be >= 2");
+                return SHG_ERR_INVALID;
+            }
+        }
+        SHG_CUDA(cudaSetDevice(crystal.device));
+        int rc = ensure_twiddles(crystal.device);
+        if (rc) return rc;
+        // Memory plan: per solve P, S, Pout, Sout, Hp, Hs (n*n float2 each), stepc (nz
+        // float4), acc (4 doubles); every block 256-byte aligned.
+        auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+        size_t total = 0;
+        std::vector<size_t> off(n);
+        for (int i = 0; i < n; ++i) {
+            off[i] = total;
+            const size_t nn = (size_t)sp[i].n * sp[i].n;
+            total += 6 * al(nn * sizeof(float2)) + al(sp[i].nz * sizeof(float4));
+        }
+        const size_t acc_off = total;
+        total += al(4 * sizeof(double) * n);
+        SHG_CUDA(cudaMalloc(&pool_, total));
+        pool_bytes_ = total;
+        acc_ = reinterpret_cast<double *>(pool_ + acc_off);
+        desc_.resize(n);
+        p_src_.assign(n, nullptr);
+        s_src_.assign(n, nullptr);
+        max_nn_ = 0;
+        max_nz_ = 0;
+        for (int i = 0; i < n; ++i) {
+            InstDesc &d = desc_[i];
+            std::memset(&d, 0, sizeof(d));
+            const size_t nn = (size_t)sp[i].n * sp[i].n, fb = al(nn * sizeof(float2));
+            char *p = pool_ + off[i];
+            d.P = reinterpret_cast<float2 *>(p);
+            d.S = reinterpret_cast<float2 *>(p + fb);
+            d.Pout = reinterpret_cast<float2 *>(p + 2 * fb);
+            d.Sout = reinterpret_cast<float2 *>(p + 3 * fb);
+            d.Hp = reinterpret_cast<float2 *>(p + 4 * fb);
+            d.Hs = reinterpret_cast<float2 *>(p + 5 * fb);
+            d.stepc = reinterpret_cast<float4 *>(p + 6 * fb);
+            d.acc = acc_ + 4 * i;
+            fill_scalars(cr_, sp[i], d);
+            max_nn_ = std::max(max_nn_, (int)nn);
+            max_nz_ = std::max(max_nz_, sp[i].nz);
+        }
+        SHG_CUDA(cudaMalloc(&d_desc_, n * sizeof(InstDesc)));
+        // Size classes, each sorted by step count (descending) so that the solves still
+        // marching at stage s form a prefix of the class list.
+        std::map<int, std::vector<int>> by_n;
+        for (int i = 0; i < n; ++i) by_n[sp[i].n].push_back(i);
+        std::vector<int> lists;
+        classes_.clear();
+        for (auto &kv : by_n) {
+            auto &v = kv.second;
+            std::stable_sort(v.begin(), v.end(), [&](int a, int b) { return desc_[a].nsteps > desc_[b].nsteps; });
+            Class c;
+            c.n = kv.first;
+            c.offset = (int)lists.size();
+            c.count = (int)v.size();
+            for (int i : v) {
+                lists.push_back(i);
+                c.steps.push_back(desc_[i].nsteps);
+            }
+            classes_.push_back(c);
+        }
+        SHG_CUDA(cudaMalloc(&d_lists_, lists.size() * sizeof(int)));
+        SHG_CUDA(cudaMemcpy(d_lists_, lists.data(), lists.size() * sizeof(int), cudaMemcpyHostToDevice));
+        SHG_CUDA(cudaMemset(pool_, 0, pool_bytes_));
+        desc_dirty_ = true;
+        return SHG_OK;
+    }
+
+    // Re-parameterise solve i (same grid) without reallocating.
+    int set_params(int i, const SolveParams &sp) {
+        if (i < 0 || i >= (int)desc_.size() || sp.n != sp_[i].n || sp.nz != sp_[i].nz) {
+            set_error("set_params: grid change needs a new handle");
+            return SHG_ERR_INVALID;
+        }
+        sp_[i] = sp;
+        const int keep_given = desc_[i].pump_given;
+        fill_scalars(cr_, sp, desc_[i]);
+        desc_[i].pump_given = keep_given;
+        desc_dirty_ = true;
+        invalidate_graph();
+        return SHG_OK;
+    }
+
+    // Device buffers copied into P / S at the start of every run (nullptr: Gaussian pump
+    // built on the device / SH cleared to zero).
+    void set_sources(int i, const float2 *p_src, const float2 *s_src) {
+        if (p_src_[i] != p_src || s_src_[i] != s_src) {
+            p_src_[i] = p_src;
+            s_src_[i] = s_src;
+            invalidate_graph();
+        }
+        const int given = p_src ? 1 : 0;
+        if (desc_[i].pump_given != given) {
+            desc_[i].pump_given = given;
+            desc_dirty_ = true;
+            invalidate_graph();
+        }
+    }
+
+    // Enqueue set-up and the march for every solve on `st` (a CUDA graph after the
+    // first call when use_graph is set).
+    int run_async(cudaStream_t st, bool use_graph) {
+        if (desc_dirty_) {
+            SHG_CUDA(cudaMemcpyAsync(d_desc_, desc_.data(), desc_.size() * sizeof(InstDesc), cudaMemcpyHostToDevice, st));
+            desc_dirty_ = false;
+        }
+        if (!use_graph) return enqueue(st);
+        if (!graph_exec_) {
+            cudaGraph_t g = nullptr;
+            SHG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            int rc = enqueue(st);
+            cudaError_t e = cudaStreamEndCapture(st, &g);
+            if (rc) {
+                if (g) cudaGraphDestroy(g);
+                return rc;
+            }
+            SHG_CUDA(e);
+            e = cudaGraphInstantiate(&graph_exec_, g, 0);
+            cudaGraphDestroy(g);
+            SHG_CUDA(e);
+        }
+        SHG_CUDA(cudaGraphLaunch(graph_exec_, st));
+        return SHG_OK;
+    }
+
+    int launch_count() const {
+        int c = 2;  // set-up kernels
+        for (const auto &k : classes_) {
+            const int K = k.steps.empty() ? 0 : k.steps[0];
+            c += (K + 1) + K;
+        }
+        return c;
+    }
+
+    int copy_acc(std::vector<double> &acc) {
+        acc.resize(4 * desc_.size());
+        SHG_CUDA(cudaMemcpy(acc.data(), acc_, acc.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        return SHG_OK;
+    }
+
+    // Efficiency of solve i from accumulated sums.
+    double eta_of(int i, const std::vector<double> &acc) const {
+        const SolveParams &s = sp_[i];
+        const float dx = desc_[i].dx, dy = desc_[i].dy;
+        const float np_c = sellmeier(cr_.lp, s.temp), ns_c = sellmeier((float)(0.5 * (double)cr_.lp), s.temp);
+        const double pin = field_power(acc[4 * i + 0], np_c, dx, dy);
+        const double psh = field_power(acc[4 * i + 1], ns_c, dx, dy);
+        return psh / pin;
+    }
+
+    void powers_of(int i, const std::vector<double> &acc, double *pin, double *psh, double *pout) const {
+        const SolveParams &s = sp_[i];
+        const float dx = desc_[i].dx, dy = desc_[i].dy;
+        const float np_c = sellmeier(cr_.lp, s.temp), ns_c = sellmeier((float)(0.5 * (double)cr_.lp), s.temp);
+        if (pin) *pin = field_power(acc[4 * i + 0], np_c, dx, dy);
+        if (psh) *psh = field_power(acc[4 * i + 1], ns_c, dx, dy);
+        if (pout) *pout = field_power(acc[4 * i + 2], np_c, dx, dy);
+    }
+
+    const InstDesc &desc(int i) const { return desc_[i]; }
+    int size() const { return (int)desc_.size(); }
+    const SolveParams &params(int i) const { return sp_[i]; }
+
+   private:
+    struct Class {
+        int n = 0, offset = 0, count = 0;
+        std::vector<int> steps;  // descending
+    };
+
+    int enqueue(cudaStream_t st) {
+        SHG_CUDA(cudaMemsetAsync(acc_, 0, 4 * sizeof(double) * desc_.size(), st));
+        for (int i = 0; i < (int)desc_.size(); ++i) {
+            const size_t bytes = (size_t)desc_[i].n * desc_[i].n * sizeof(float2);
+            if (p_src_[i]) SHG_CUDA(cudaMemcpyAsync(desc_[i].P, p_src_[i], bytes, cudaMemcpyDeviceToDevice, st));
+            if (s_src_[i])
+                SHG_CUDA(cudaMemcpyAsync(desc_[i].S, s_src_[i], bytes, cudaMemcpyDeviceToDevice, st));
+            else
+                SHG_CUDA(cudaMemsetAsync(desc_[i].S, 0, bytes, st));
+        }
+        SHG_CUDA(launch_setup(d_desc_, (int)desc_.size(), max_nn_, max_nz_, st));
+        for (const auto &k : classes_) {
+            const int K = k.steps[0];
+            const int *list = d_lists_ + k.offset;
+            for (int s = 0; s <= K; ++s) {
+                // solves with nsteps >= s run the row pass, nsteps >= s + 1 the column pass
+                const int nr = count_at_least(k.steps, s), nc = count_at_least(k.steps, s + 1);
+                SHG_CUDA(launch_rows(k.n, d_desc_, list, nr, s, st));
+                if (nc > 0) SHG_CUDA(launch_cols(k.n, d_desc_, list, nc, st));
+            }
+        }
+        return SHG_OK;
+    }
+
+    static int count_at_least(const std::vector<int> &desc_sorted, int v) {
+        // desc_sorted is descending: count of entries >= v
+        int lo = 0, hi = (int)desc_sorted.size();
+        while (lo < hi) {
+            const int mid = (lo + hi) / 2;
+            if (desc_sorted[mid] >= v)
+                lo = mid + 1;
+            else
+                hi = mid;
+        }
+        return lo;
+    }
+
+    void invalidate_graph() {
+        if (graph_exec_) {
+            cudaGraphExecDestroy(graph_exec_);
+            graph_exec_ = nullptr;
+        }
+    }
+
+    void release() {
+        invalidate_graph();
+        if (pool_) cudaFree(pool_);
+        if (d_desc_) cudaFree(d_desc_);
+        if (d_lists_) cudaFree(d_lists_);
+        pool_ = nullptr;
+        d_desc_ = nullptr;
+        d_lists_ = nullptr;
+    }
+
+    shg_config cr_{};
+    std::vector<SolveParams> sp_;
+    std::vector<InstDesc> desc_;
+    std::vector<const float2 *> p_src_, s_src_;
+    std::vector<Class> classes_;
+    char *pool_ = nullptr;
+    size_t pool_bytes_ = 0;
+    double *acc_ = nullptr;
+    InstDesc *d_desc_ = nullptr;
+    int *d_lists_ = nullptr;
+    int max_nn_ = 0, max_nz_ = 0;
+    bool desc_dirty_ = true;
+    cudaGraphExec_t graph_exec_ = nullptr;
+};
+
+int validate_config(const shg_config &c) {
+    if (c.nx <= 1 || c.ny <= 1 || c.nz <= 1) {
+        set_error("grid sizes must be > 1");
+        return SHG_ERR_INVALID;
+    }
+    if (!(c.lx > 0) || !(c.ly > 0) || !(c.lz > 0) || !(c.lp > 0) || !(c.lambda_qpm != 0)) {
+        set_error("window, crystal length, wavelength and poling period must be positive");
+        return SHG_ERR_INVALID;
+    }
+    if (c.nx != c.ny || !line_length_supported(c.nx)) {
+        set_error("the device path needs a square grid with NX = NY a power of two in [16, 256]");
+        return SHG_ERR_UNSUPPORTED;
+    }
+    return SHG_OK;
+}
+
+}  // namespace shg
+
+using namespace shg;
+
+struct shg_handle {
+    shg_config cfg;
+    Batch batch;
+    SolveParams sp{};
+    int n = 0;
+    float2 *stage_p = nullptr, *stage_s = nullptr;  // device staging of given input fields
+    bool pump_given = false, sh_given = false, have_pump = false, have_result = false;
+    cudaStream_t stream = nullptr;
+    ~shg_handle() {
+        if (stage_p) cudaFree(stage_p);
+        if (stage_s) cudaFree(stage_s);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+struct shg_batch {
+    shg_config cfg;
+    Batch batch;
+    cudaStream_t stream = nullptr;
+    bool ran = false;
+    ~shg_batch() {
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+// Efields.h:129-144 with a fixed seed: std::default_random_engine and
+// std::normal_distribution<float>(0, 1e-20), two draws per point (re, im).
+void noise_field(unsigned seed, size_t n, std::vector<float2> &out) {
+    std::default_random_engine generator(seed);
+    std::normal_distribution<float> distribution(0.0, 1.0e-20);
+    out.resize(n);
+    for (size_t i = 0; i < n; ++i) {
+        const float a1 = distribution(generator);
+        const float a2 = distribution(generator);
+        out[i] = make_float2(a1, a2);
+    }
+}
+
+int handle_run(shg_handle *h, cudaStream_t st) {
+    Batch &b = h->batch;
+    int rc = b.set_params(0, h->sp);
+    if (rc) return rc;
+    b.set_sources(0, h->pump_given ? h->stage_p : nullptr, h->sh_given ? h->stage_s : nullptr);
+    rc = b.run_async(st, true);
+    if (rc) return rc;
+    h->have_result = true;
+    return SHG_OK;
+}
+
+int check_handle(shg_handle *h) {
+    if (!h) {
+        set_error("null handle");
+        return SHG_ERR_INVALID;
+    }
+    return SHG_OK;
+}
+
+}  // namespace
+
+#define SHG_TRY(expr)          \
+    do {                       \
+        int rc_ = (expr);      \
+        if (rc_) return rc_;   \
+    } while (0)
+
+extern "C" {
+
+int shg_config_init(shg_config *c) {
+    if (!c) {
+        set_error("null config");
+        return SHG_ERR_INVALID;
+    }
+    std::memset(c, 0, sizeof(*c));
+    c->nx = 64;
+    c->ny = 64;
+    c->nz = 200;
+    c->lx = 2000.0f;
+    c->ly = 1000.0f;
+    c->lz = 30000.0f;
+    c->lp = 1.064f;
+    c->deff = 11.00e-6f;
+    c->lambda_qpm = 7.97f;
+    c->alpha_p = 0.17e-6f;
+    c->alpha_s = 1.57e-6f;
+    c->beta_s = 5e-5f;
+    c->rho_p = 0.0f;
+    c->rho_s = 0.0f;
+    c->kth = 8.4e-6f;
+    c->htc = 10e-12f;
+    c->thermal = 0;
+    c->bc = 0;
+    c->sh_seed = -1;
+    c->device = 0;
+    return SHG_OK;
+}
+
+const char *shg_last_error(void) { return g_last_error.c_str(); }
+
+int shg_create(const shg_config *cfg, shg_handle **out) {
+    if (!cfg || !out) {
+        set_error("null argument");
+        return SHG_ERR_INVALID;
+    }
+    *out = nullptr;
+    SHG_TRY(validate_config(*cfg));
+    if (cfg->thermal) {
+        set_error("THERMAL runs are not available in this build");
+        return SHG_ERR_UNSUPPORTED;
+    }
+    auto *h = new shg_handle;
+    h->cfg = *cfg;
+    h->n = cfg->nx;
+    h->sp = SolveParams{cfg->nx, cfg->nz, cfg->lx, cfg->ly, 1.0f, 30.0f, 0.5f * cfg->lz, 50.0f, 50.0f, 50.0f};
+    int rc = h->batch.create(*cfg, {h->sp});
+    if (rc) {
+        delete h;
+        return rc;
+    }
+    const size_t bytes = (size_t)h->n * h->n * sizeof(float2);
+    if (cudaMalloc(&h->stage_p, bytes) != cudaSuccess || cudaMalloc(&h->stage_s, bytes) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        set_error("device allocation for the handle failed");
+        delete h;
+        return SHG_ERR_NOMEM;
+    }
+    *out = h;
+    return SHG_OK;
+}
+
+int shg_destroy(shg_handle *h) {
+    delete h;
+    return SHG_OK;
+}
+
+int shg_set_input_pump(shg_handle *h, float power, float focalpoint, float waist, float tc) {
+    SHG_TRY(check_handle(h));
+    h->sp.power = power;
+    h->sp.focal = focalpoint;
+    h->sp.waist = waist;
+    h->sp.tpump = tc;
+    h->pump_given = false;
+    h->have_pump = true;
+    return SHG_OK;
+}
+
+int shg_set_input_fields(shg_handle *h, const float *pump, const float *sh) {
+    SHG_TRY(check_handle(h));
+    if (!pump) {
+        set_error("pump field required");
+        return SHG_ERR_INVALID;
+    }
+    const size_t bytes = (size_t)h->n * h->n * sizeof(float2);
+    SHG_CUDA(cudaMemcpy(h->stage_p, pump, bytes, cudaMemcpyHostToDevice));
+    h->pump_given = true;
+    h->have_pump = true;
+    if (sh) {
+        SHG_CUDA(cudaMemcpy(h->stage_s, sh, bytes, cudaMemcpyHostToDevice));
+        h->sh_given = true;
+    } else {
+        h->sh_given = false;
+    }
+    return SHG_OK;
+}
+
+int shg_cwes(shg_handle *h, float temp) {
+    SHG_TRY(check_handle(h));
+    if (!h->have_pump) {
+        set_error("shg_cwes: no input pump (shg_set_input_pump or shg_set_input_fields first)");
+        return SHG_ERR_STATE;
+    }
+    h->sp.temp = temp;
+    h->sp.tprop = temp;
+    SHG_TRY(handle_run(h, h->stream));
+    SHG_CUDA(cudaStreamSynchronize(h->stream));
+    return SHG_OK;
+}
+
+int shg_cwes_device(shg_handle *h, float temp, const void *pump_in, const void *sh_in, void *pump_out,
+                    void *sh_out, void *stream) {
+    SHG_TRY(check_handle(h));
+    if (!pump_in) {
+        set_error("pump_in required");
+        return SHG_ERR_INVALID;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t bytes = (size_t)h->n * h->n * sizeof(float2);
+    SHG_CUDA(cudaMemcpyAsync(h->stage_p, pump_in, bytes, cudaMemcpyDeviceToDevice, st));
+    if (sh_in) SHG_CUDA(cudaMemcpyAsync(h->stage_s, sh_in, bytes, cudaMemcpyDeviceToDevice, st));
+    h->pump_given = true;
+    h->sh_given = sh_in != nullptr;
+    h->have_pump = true;
+    h->sp.temp = temp;
+    h->sp.tprop = temp;
+    SHG_TRY(handle_run(h, st));
+    const InstDesc &d = h->batch.desc(0);
+    if (pump_out) SHG_CUDA(cudaMemcpyAsync(pump_out, d.Pout, bytes, cudaMemcpyDeviceToDevice, st));
+    if (sh_out) SHG_CUDA(cudaMemcpyAsync(sh_out, d.Sout, bytes, cudaMemcpyDeviceToDevice, st));
+    return SHG_OK;
+}
+
+int shg_run(shg_handle *h, float power, float waist, float focalpoint, float temp, float t_inf, float t_peltier1,
+            float t_peltier2, int save_only_last, int save_temperature) {
+    SHG_TRY(check_handle(h));
+    (void)t_inf;
+    (void)t_peltier1;
+    (void)t_peltier2;
+    (void)save_only_last;
+    (void)save_temperature;
+    // Solver.h:342-348: pump, SH start, propagators and delta-k all at Temp.
+    h->sp.power = power;
+    h->sp.waist = waist;
+    h->sp.focal = focalpoint;
+    h->sp.temp = temp;
+    h->sp.tpump = temp;
+    h->sp.tprop = temp;
+    h->pump_given = false;
+    h->have_pump = true;
+    if (h->cfg.sh_seed >= 0) {
+        std::vector<float2> nz;
+        noise_field((unsigned)h->cfg.sh_seed, (size_t)h->n * h->n, nz);
+        SHG_CUDA(cudaMemcpy(h->stage_s, nz.data(), nz.size() * sizeof(float2), cudaMemcpyHostToDevice));
+        h->sh_given = true;
+    } else {
+        h->sh_given = false;
+    }
+    SHG_TRY(handle_run(h, h->stream));
+    SHG_CUDA(cudaStreamSynchronize(h->stream));
+    return SHG_OK;
+}
+
+int shg_get_fields(shg_handle *h, float *pump_out, float *sh_out) {
+    SHG_TRY(check_handle(h));
+    if (!h->have_result) {
+        set_error("no result yet");
+        return SHG_ERR_STATE;
+    }
+    const InstDesc &d = h->batch.desc(0);
+    const size_t bytes = (size_t)h->n * h->n * sizeof(float2);
+    SHG_CUDA(cudaStreamSynchronize(h->stream));
+    if (pump_out) SHG_CUDA(cudaMemcpy(pump_out, d.Pout, bytes, cudaMemcpyDeviceToHost));
+    if (sh_out) SHG_CUDA(cudaMemcpy(sh_out, d.Sout, bytes, cudaMemcpyDeviceToHost));
+    return SHG_OK;
+}
+
+int shg_get_powers(shg_handle *h, double *p_pump_in, double *p_sh_out, double *p_pump_out) {
+    SHG_TRY(check_handle(h));
+    if (!h->have_result) {
+        set_error("no result yet");
+        return SHG_ERR_STATE;
+    }
+    std::vector<double> acc;
+    SHG_CUDA(cudaDeviceSynchronize());
+    SHG_TRY(h->batch.copy_acc(acc));
+    h->batch.powers_of(0, acc, p_pump_in, p_sh_out, p_pump_out);
+    return SHG_OK;
+}
+
+int shg_efficiency(shg_handle *h, double *eta) {
+    double pin = 0, psh = 0;
+    SHG_TRY(shg_get_powers(h, &pin, &psh, nullptr));
+    *eta = psh / pin;
+    if (!std::isfinite(*eta)) {
+        set_error("efficiency is not finite");
+        return SHG_ERR_NONFINITE;
+    }
+    return SHG_OK;
+}
+
+int shg_batch_create(const shg_config *crystal, const shg_instance *inst, int n, shg_batch **out) {
+    if (!crystal || !inst || !out || n <= 0) {
+        set_error("null argument or empty batch");
+        return SHG_ERR_INVALID;
+    }
+    *out = nullptr;
+    std::vector<SolveParams> sp(n);
+    for (int i = 0; i < n; ++i) {
+        const shg_instance &s = inst[i];
+        if (s.nx != s.ny) {
+            set_error("batch solves must be square");
+            return SHG_ERR_UNSUPPORTED;
+        }
+        sp[i] = SolveParams{s.nx, s.nz, s.lx, s.ly, s.power, s.waist, s.focal, s.temp, s.temp, s.temp};
+    }
+    auto *b = new shg_batch;
+    b->cfg = *crystal;
+    int rc = b->batch.create(*crystal, sp);
+    if (rc) {
+        delete b;
+        return rc;
+    }
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        set_error("stream creation failed");
+        delete b;
+        return SHG_ERR_CUDA;
+    }
+    *out = b;
+    return SHG_OK;
+}
+
+int shg_batch_destroy(shg_batch *b) {
+    delete b;
+    return SHG_OK;
+}
+
+int shg_batch_run_async(shg_batch *b, void *stream) {
+    if (!b) {
+        set_error("null batch");
+        return SHG_ERR_INVALID;
+    }
+    SHG_TRY(b->batch.run_async(static_cast<cudaStream_t>(stream), true));
+    b->ran = true;
+    return SHG_OK;
+}
+
+int shg_batch_results(shg_batch *b, double *eta) {
+    if (!b || !eta) {
+        set_error("null argument");
+        return SHG_ERR_INVALID;
+    }
+    if (!b->ran) {
+        set_error("batch has not run");
+        return SHG_ERR_STATE;
+    }
+    std::vector<double> acc;
+    SHG_TRY(b->batch.copy_acc(acc));
+    for (int i = 0; i < b->batch.size(); ++i) eta[i] = b->batch.eta_of(i, acc);
+    return SHG_OK;
+}
+
+int shg_batch_run(shg_batch *b, double *eta, float **fields_out) {
+    if (!b) {
+        set_error("null batch");
+        return SHG_ERR_INVALID;
+    }
+    SHG_TRY(b->batch.run_async(b->stream, true));
+    b->ran = true;
+    SHG_CUDA(cudaStreamSynchronize(b->stream));
+    if (eta) SHG_TRY(shg_batch_results(b, eta));
+    if (fields_out) {
+        for (int i = 0; i < b->batch.size(); ++i) {
+            if (!fields_out[i]) continue;
+            const InstDesc &d = b->batch.desc(i);
+            SHG_CUDA(cudaMemcpyAsync(fields_out[i], d.Sout, (size_t)d.n * d.n * sizeof(float2),
+                                     cudaMemcpyDeviceToHost, b->stream));
+        }
+        SHG_CUDA(cudaStreamSynchronize(b->stream));
+    }
+    return SHG_OK;
+}
+
+int shg_batch_launch_count(shg_batch *b, int *launches) {
+    if (!b || !launches) {
+        set_error("null argument");
+        return SHG_ERR_INVALID;
+    }
+    *launches = b->batch.launch_count();
+    return SHG_OK;
+}
+
+int shg_dft2d_device(int n, int sign, const void *in, void *out, void *stream) {
+    if (!line_length_supported(n) || (sign != 1 && sign != -1) || !in || !out) {
+        set_error("shg_dft2d_device: unsupported size or bad argument");
+        return SHG_ERR_INVALID;
+    }
+    int dev = 0;
+    SHG_CUDA(cudaGetDevice(&dev));
+    SHG_TRY(ensure_twiddles(dev));
+    SHG_CUDA(launch_dft2d(n, sign, static_cast<const float2 *>(in), static_cast<float2 *>(out),
+                          static_cast<cudaStream_t>(stream)));
+    return SHG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,332 @@
+// Plain SSFM z-march kernels (Solver.h:236-276 without THERMAL), batched over solves.
+//
+// One SSFM step of the reference is RK4(z) -> diffraction -> RK4(z) (Solver.h:236-242),
+// where diffraction is FFT_backward -> propagator product -> FFT_forward -> 1/(NX*NY)
+// (Solver.h:156-190). The march here regroups the work of consecutive steps into two
+// passes per step so that each field crosses memory twice per step:
+//
+//   row pass (k_rows, lines along x): finish the forward 2D transform of step s-1 along x,
+//       second RK4 of step s-1, [capture at the top of slice nz-1], first RK4 of step s,
+//       start the backward 2D transform of step s along x;
+//   column pass (k_cols, lines along y): backward transform along y, product with the
+//       shifted propagator (pre-scaled by 1/(NX*NY), exact for power-of-two grids), forward
+//       transform along y.
+//
+// The row-pass transforms use the spectral register layout between the forward and the
+// backward transform, so the RK4 work never reorders data (shg_fft.cuh).
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "shg_internal.h"
+#include "shg_march.cuh"
+
+namespace shg {
+
+// Twiddle tables exp(-2 pi i m / N): the table for line length N sits at [N, 2N).
+__device__ float2 g_twiddle[2 * kMaxLine];
+
+const float2 *twiddle_symbol_address() {
+    void *p = nullptr;
+    cudaGetSymbolAddress(&p, g_twiddle);
+    return static_cast<const float2 *>(p);
+}
+
+// ---------------------------------------------------------------------------------------
+// Setup: phase table, Gaussian pump, shifted propagators, input power.
+
+// z accumulates in float (Solver.h:271), one thread walks the slices of one solve; the
+// phase exp(-+ i z dk) enters dA/dz through cosf/sinf of fl(z*dk) (Operators.h:105-117).
+__global__ void k_setup_steps(const InstDesc *__restrict__ inst, int n_inst) {
+    extern __shared__ float zs[];
+    const InstDesc &d = inst[blockIdx.x];
+    if (threadIdx.x == 0) {
+        float z = 0.0f;
+        for (int s = 0; s < d.nz; ++s) {
+            zs[s] = z;
+            z = __fadd_rn(z, d.dz);
+        }
+    }
+    __syncthreads();
+    for (int s = threadIdx.x; s < d.nz; s += blockDim.x) {
+        const float arg = __fmul_rn(zs[s], d.dk);
+        float sn, cs;
+        sincosf(arg, &sn, &cs);
+        d.stepc[s] = make_float4(d.kp * sn, d.kp * cs, -d.ks * sn, d.ks * cs);
+    }
+}
+
+__device__ __forceinline__ void block_add_double(double v, double *dst) {
+    __shared__ double red[32];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = (l < (int)(blockDim.x >> 5)) ? red[l] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (l == 0 && v != 0.0) atomicAdd(dst, v);
+    }
+}
+
+// Efields.h:74-104 (pump) and Efields.h:107-126 + 32-71 (propagators), with the float
+// operations of the reference kept in order (no contraction); only cosf/sinf/expf are the
+// device's. Grid: (chunks of 4*blockDim pixels, solves).
+__global__ void k_setup_fields(const InstDesc *__restrict__ inst) {
+    const InstDesc &d = inst[blockIdx.y];
+    const int n = d.n, nn = n * n, half = n / 2;
+    double acc = 0.0;
+    for (int q = 0; q < 4; ++q) {
+        const int i = (blockIdx.x * 4 + q) * blockDim.x + threadIdx.x;
+        if (i >= nn) break;
+        const int ix = i % n, iy = i / n;
+        if (!d.pump_given) {
+            const float ax = __fmul_rn(__fsub_rn((float)ix, d.uX), d.dx);
+            const float ay = __fmul_rn(__fsub_rn((float)iy, d.uY), d.dy);
+            const float num = __fsub_rn(-__fmul_rn(ax, ax), __fmul_rn(ay, ay));
+            const float re = __fdiv_rn(__fmul_rn(num, d.wM.x), d.wM_den);
+            const float im = __fdiv_rn(__fmul_rn(-num, d.wM.y), d.wM_den);
+            const float e = expf(re);
+            float sn, cs;
+            sincosf(im, &sn, &cs);
+            const float er = __fmul_rn(e, cs), ei = __fmul_rn(e, sn);
+            const float2 p = make_float2(__fsub_rn(__fmul_rn(d.amp.x, er), __fmul_rn(d.amp.y, ei)),
+                                         __fadd_rn(__fmul_rn(d.amp.x, ei), __fmul_rn(d.amp.y, er)));
+            d.P[i] = p;
+        }
+        const float2 p = d.P[i];
+        acc += (double)p.x * p.x + (double)p.y * p.y;
+        // shifted propagator: H_shift[ix, iy] = H[(ix + n/2) % n, (iy + n/2) % n]
+        const int ux = (ix + half) & (n - 1), uy = (iy + half) & (n - 1);
+        const float tx = __fsub_rn((float)ux, d.uX), ty = __fsub_rn((float)uy, d.uY);
+        const float q2 = __fadd_rn(__fmul_rn(d.dfX2, __fmul_rn(tx, tx)), __fmul_rn(d.dfY2, __fmul_rn(ty, ty)));
+        const float php = __fmul_rn(d.mdz, __fadd_rn(__fmul_rn(d.gp, q2), __fmul_rn(d.linp, tx)));
+        const float phs = __fmul_rn(d.mdz, __fadd_rn(__fmul_rn(d.gs, q2), __fmul_rn(d.lins, tx)));
+        float s1, c1, s2, c2;
+        sincosf(php, &s1, &c1);
+        sincosf(phs, &s2, &c2);
+        d.Hp[i] = make_float2(c1 * d.inv_nn, s1 * d.inv_nn);
+        d.Hs[i] = make_float2(c2 * d.inv_nn, s2 * d.inv_nn);
+    }
+    block_add_double(acc, d.acc + 0);
+}
+
+// ---------------------------------------------------------------------------------------
+// Row pass. Block = 256 threads = 256/G lines of one solve; mode from the stage s:
+//   s == 0           : RK4(z_0), backward transform along x, store in frequency order;
+//   0 < s < nsteps   : forward transform along x, RK4(z_{s-1}), RK4(z_s), backward;
+//   s == nsteps      : forward transform along x, RK4(z_{s-1}), capture, power sums.
+template <int N>
+struct RowShape {
+    static constexpr int G = LineShape<N>::G;
+    static constexpr int TPB = (N * G < 256) ? N * G : 256;  // threads per block
+    static constexpr int LPB = TPB / G;                      // lines per block
+    static constexpr int BPI = N / LPB;                      // blocks per solve
+};
+
+template <int N>
+__global__ void __launch_bounds__(RowShape<N>::TPB) k_rows(const InstDesc *__restrict__ inst, const int *__restrict__ list, int s) {
+    constexpr int G = LineShape<N>::G, E = N / G, LPB = RowShape<N>::LPB, BPI = RowShape<N>::BPI;
+    constexpr int SC = LineScratch<N, G>::SIZE;
+    static_assert(N % LPB == 0, "blocks must not straddle solves");
+    __shared__ float2 scratch[LPB * SC];
+    const InstDesc &d = inst[list[blockIdx.x / BPI]];
+    const float2 *__restrict__ tab = g_twiddle + N;
+    const int line = (blockIdx.x % BPI) * LPB + threadIdx.x / G;
+    const int t = threadIdx.x % G;
+    float2 *sc = scratch + (threadIdx.x / G) * SC;
+    const size_t base = (size_t)line * N;
+    float2 vp[E], vs[E];
+#pragma unroll
+    for (int j = 0; j < E; ++j) {
+        vp[j] = d.P[base + t + G * j];
+        vs[j] = d.S[base + t + G * j];
+    }
+    if (s == 0) {
+        const float4 c = d.stepc[0];
+#pragma unroll
+        for (int j = 0; j < E; ++j) rk4_point(vp[j], vs[j], c, d);
+        fft_nat_to_spec<N, G, +1>(vp, t, sc, tab);
+        fft_nat_to_spec<N, G, +1>(vs, t, sc, tab);
+#pragma unroll
+        for (int r = 0; r < E; ++r) {
+            const int k = spec_index<N, G>(t, r);
+            d.P[base + k] = vp[r];
+            d.S[base + k] = vs[r];
+        }
+        return;
+    }
+    fft_nat_to_spec<N, G, -1>(vp, t, sc, tab);
+    fft_nat_to_spec<N, G, -1>(vs, t, sc, tab);
+    const float4 c1 = d.stepc[s - 1];
+#pragma unroll
+    for (int r = 0; r < E; ++r) rk4_point(vp[r], vs[r], c1, d);
+    if (s == d.nsteps) {
+        double aS = 0.0, aP = 0.0;
+#pragma unroll
+        for (int r = 0; r < E; ++r) {
+            const int k = spec_index<N, G>(t, r);
+            d.Pout[base + k] = vp[r];
+            d.Sout[base + k] = vs[r];
+            aS += (double)vs[r].x * vs[r].x + (double)vs[r].y * vs[r].y;
+            aP += (double)vp[r].x * vp[r].x + (double)vp[r].y * vp[r].y;
+        }
+        block_add_double(aS, d.acc + 1);
+        block_add_double(aP, d.acc + 2);
+        return;
+    }
+    const float4 c2 = d.stepc[s];
+#pragma unroll
+    for (int r = 0; r < E; ++r) rk4_point(vp[r], vs[r], c2, d);
+    fft_spec_to_nat<N, G, +1>(vp, t, sc, tab);
+    fft_spec_to_nat<N, G, +1>(vs, t, sc, tab);
+#pragma unroll
+    for (int j = 0; j < E; ++j) {
+        d.P[base + t + G * j] = vp[j];
+        d.S[base + t + G * j] = vs[j];
+    }
+}
+
+// Column pass. Block = TC columns x G threads (lane = column + TC * t) so that every
+// load and store is a run of TC consecutive complex values.
+template <int N>
+__global__ void __launch_bounds__(16 * LineShape<N>::G) k_cols(const InstDesc *__restrict__ inst, const int *__restrict__ list) {
+    constexpr int G = LineShape<N>::G, E = N / G, TC = 16, BPI = N / TC;
+    __shared__ float2 scratch[TC * E * G];
+    const InstDesc &d = inst[list[blockIdx.x / BPI]];
+    const float2 *__restrict__ tab = g_twiddle + N;
+    const int c = threadIdx.x % TC, t = threadIdx.x / TC;
+    const int x = (blockIdx.x % BPI) * TC + c;
+    float2 *sc = scratch + c;
+#pragma unroll 1
+    for (int f = 0; f < 2; ++f) {
+        float2 *F = f == 0 ? d.P : d.S;
+        const float2 *__restrict__ H = f == 0 ? d.Hp : d.Hs;
+        float2 v[E];
+#pragma unroll
+        for (int j = 0; j < E; ++j) v[j] = F[(size_t)(t + G * j) * N + x];
+        fft_nat_to_spec<N, G, +1, true, TC, G>(v, t, sc, tab);
+#pragma unroll
+        for (int r = 0; r < E; ++r) {
+            const int k = spec_index<N, G>(t, r);
+            v[r] = c_mul(v[r], __ldg(H + (size_t)k * N + x));
+        }
+        fft_spec_to_nat<N, G, -1, true, TC, G>(v, t, sc, tab);
+#pragma unroll
+        for (int j = 0; j < E; ++j) F[(size_t)(t + G * j) * N + x] = v[j];
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Standalone unnormalised 2D DFT (component tests): rows, then columns in place on out.
+template <int N, int SIGN>
+__global__ void __launch_bounds__(RowShape<N>::TPB) k_dft_rows(const float2 *__restrict__ in, float2 *out) {
+    constexpr int G = LineShape<N>::G, E = N / G, LPB = RowShape<N>::LPB;
+    constexpr int SC = LineScratch<N, G>::SIZE;
+    __shared__ float2 scratch[LPB * SC];
+    const float2 *__restrict__ tab = g_twiddle + N;
+    const int line = blockIdx.x * LPB + threadIdx.x / G, t = threadIdx.x % G;
+    float2 *sc = scratch + (threadIdx.x / G) * SC;
+    float2 v[E];
+#pragma unroll
+    for (int j = 0; j < E; ++j) v[j] = in[(size_t)line * N + t + G * j];
+    fft_nat_to_spec<N, G, SIGN>(v, t, sc, tab);
+#pragma unroll
+    for (int r = 0; r < E; ++r) out[(size_t)line * N + spec_index<N, G>(t, r)] = v[r];
+}
+
+template <int N, int SIGN>
+__global__ void __launch_bounds__(16 * LineShape<N>::G) k_dft_cols(float2 *out) {
+    constexpr int G = LineShape<N>::G, E = N / G, TC = 16;
+    __shared__ float2 scratch[TC * E * G];
+    const float2 *__restrict__ tab = g_twiddle + N;
+    const int c = threadIdx.x % TC, t = threadIdx.x / TC, x = blockIdx.x * TC + c;
+    float2 v[E];
+#pragma unroll
+    for (int j = 0; j < E; ++j) v[j] = out[(size_t)(t + G * j) * N + x];
+    fft_nat_to_spec<N, G, SIGN, true, TC, G>(v, t, scratch + c, tab);
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < E; ++r) out[(size_t)spec_index<N, G>(t, r) * N + x] = v[r];
+}
+
+template <int N>
+static cudaError_t launch_dft2d_t(int sign, const float2 *in, float2 *out, cudaStream_t st) {
+    constexpr int G = LineShape<N>::G, TC = 16;
+    constexpr int rb = RowShape<N>::BPI, tpb = RowShape<N>::TPB;
+    if (sign < 0) {
+        k_dft_rows<N, -1><<<rb, tpb, 0, st>>>(in, out);
+        k_dft_cols<N, -1><<<N / TC, TC * G, 0, st>>>(out);
+    } else {
+        k_dft_rows<N, +1><<<rb, tpb, 0, st>>>(in, out);
+        k_dft_cols<N, +1><<<N / TC, TC * G, 0, st>>>(out);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dft2d(int n, int sign, const float2 *in, float2 *out, cudaStream_t st) {
+    switch (n) {
+        case 16: return launch_dft2d_t<16>(sign, in, out, st);
+        case 32: return launch_dft2d_t<32>(sign, in, out, st);
+        case 64: return launch_dft2d_t<64>(sign, in, out, st);
+        case 128: return launch_dft2d_t<128>(sign, in, out, st);
+        case 256: return launch_dft2d_t<256>(sign, in, out, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Host-side launchers.
+
+int rows_threads() { return 256; }
+
+template <int N>
+static cudaError_t launch_rows_t(const InstDesc *inst, const int *list, int count, int s, cudaStream_t st) {
+    if (count <= 0) return cudaSuccess;
+    k_rows<N><<<count * RowShape<N>::BPI, RowShape<N>::TPB, 0, st>>>(inst, list, s);
+    return cudaGetLastError();
+}
+
+template <int N>
+static cudaError_t launch_cols_t(const InstDesc *inst, const int *list, int count, cudaStream_t st) {
+    constexpr int G = LineShape<N>::G, TC = 16, BPI = N / TC;
+    if (count <= 0) return cudaSuccess;
+    k_cols<N><<<count * BPI, TC * G, 0, st>>>(inst, list);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rows(int n, const InstDesc *inst, const int *list, int count, int s, cudaStream_t st) {
+    switch (n) {
+        case 16: return launch_rows_t<16>(inst, list, count, s, st);
+        case 32: return launch_rows_t<32>(inst, list, count, s, st);
+        case 64: return launch_rows_t<64>(inst, list, count, s, st);
+        case 128: return launch_rows_t<128>(inst, list, count, s, st);
+        case 256: return launch_rows_t<256>(inst, list, count, s, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_cols(int n, const InstDesc *inst, const int *list, int count, cudaStream_t st) {
+    switch (n) {
+        case 16: return launch_cols_t<16>(inst, list, count, st);
+        case 32: return launch_cols_t<32>(inst, list, count, st);
+        case 64: return launch_cols_t<64>(inst, list, count, st);
+        case 128: return launch_cols_t<128>(inst, list, count, st);
+        case 256: return launch_cols_t<256>(inst, list, count, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_setup(const InstDesc *inst, int n_inst, int max_nn, int max_nz, cudaStream_t st) {
+    if (n_inst <= 0) return cudaSuccess;
+    k_setup_steps<<<n_inst, 256, (size_t)max_nz * sizeof(float), st>>>(inst, n_inst);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    dim3 grid((max_nn + 1023) / 1024, n_inst);
+    k_setup_fields<<<grid, 256, 0, st>>>(inst);
+    return cudaGetLastError();
+}
+
+bool line_length_supported(int n) { return n == 16 || n == 32 || n == 64 || n == 128 || n == 256; }
+
+}  // namespace shg

@@ -1,0 +1,181 @@
+"""Python mirror of the reference's solver interface over the C ABI.
+
+``Solver`` follows ``class Solver`` of Solver.h:120-153 (``run`` with the arguments of
+Solver::run, Solver.h:279) plus the set-up calls of Efields (Efields.h:174-192) and the
+plain CWES (Solver.h:245). ``Sweep`` runs many independent solves in one device schedule
+(the SHG.sh one-process-per-point loop, SHG.sh:39-90). Host arrays are numpy complex64
+of shape (NY, NX) in the reference layout IDX(x, y) = y*NX + x.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import asdict, is_dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, lib
+
+
+def _cfg_from(crystal=None, **kw) -> _lib.Config:
+    cfg = _lib.default_config()
+    if crystal is not None:
+        src = asdict(crystal) if is_dataclass(crystal) else dict(crystal)
+        for k in ("lx", "ly", "lz", "lp", "deff", "lambda_qpm", "alpha_p", "alpha_s", "beta_s", "rho_p",
+                  "rho_s", "kth", "htc"):
+            if k in src:
+                setattr(cfg, k, float(src[k]))
+    for k, v in kw.items():
+        setattr(cfg, k, v)
+    return cfg
+
+
+def _pf(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class Solver:
+    """One solve on the device (Solver.h:120-153)."""
+
+    def __init__(self, crystal=None, nx=64, ny=64, nz=200, lx=None, ly=None, thermal=False, bc=0, sh_seed=-1,
+                 device=0):
+        kw = dict(nx=nx, ny=ny, nz=nz, thermal=int(thermal), bc=bc, sh_seed=sh_seed, device=device)
+        if lx is not None:
+            kw["lx"] = float(lx)
+        if ly is not None:
+            kw["ly"] = float(ly)
+        self.cfg = _cfg_from(crystal, **kw)
+        h = C.c_void_p()
+        check(lib().shg_create(C.byref(self.cfg), C.byref(h)), "shg_create")
+        self._h = h
+        self.nx, self.ny, self.nz = nx, ny, nz
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().shg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # Solver::run (Solver.h:279)
+    def run(self, power, waist, focalpoint, temp, t_inf=25.0, t_peltier1=None, t_peltier2=None,
+            save_only_last=True, save_temperature=False):
+        t1 = temp if t_peltier1 is None else t_peltier1
+        t2 = t1 if t_peltier2 is None else t_peltier2
+        check(lib().shg_run(self._h, power, waist, focalpoint, temp, t_inf, t1, t2, int(save_only_last),
+                            int(save_temperature)), "shg_run")
+        return self
+
+    # Efields::setInputPump (Efields.h:174)
+    def set_input_pump(self, power, focalpoint, waist, tc):
+        check(lib().shg_set_input_pump(self._h, power, focalpoint, waist, tc), "shg_set_input_pump")
+
+    def set_input_fields(self, pump: np.ndarray, sh: np.ndarray | None = None):
+        p = np.ascontiguousarray(pump, np.complex64)
+        s = None if sh is None else np.ascontiguousarray(sh, np.complex64)
+        check(lib().shg_set_input_fields(self._h, _pf(p), None if s is None else _pf(s)), "shg_set_input_fields")
+
+    # Solver::CWES (Solver.h:245), plain
+    def cwes(self, temp):
+        check(lib().shg_cwes(self._h, temp), "shg_cwes")
+        return self
+
+    def cwes_device(self, temp, pump_in, sh_in=None, pump_out=None, sh_out=None, stream=None):
+        """Device-pointer CWES on torch tensors (complex64, (NY, NX), contiguous)."""
+        import torch
+        if pump_out is None:
+            pump_out = torch.empty_like(pump_in)
+        if sh_out is None:
+            sh_out = torch.empty_like(pump_in)
+        st = torch.cuda.current_stream(pump_in.device).cuda_stream if stream is None else stream
+        check(lib().shg_cwes_device(self._h, temp, pump_in.data_ptr(),
+                                    None if sh_in is None else sh_in.data_ptr(), pump_out.data_ptr(),
+                                    sh_out.data_ptr(), st), "shg_cwes_device")
+        return pump_out, sh_out
+
+    def fields(self):
+        p = np.zeros((self.ny, self.nx), np.complex64)
+        s = np.zeros((self.ny, self.nx), np.complex64)
+        check(lib().shg_get_fields(self._h, _pf(p), _pf(s)), "shg_get_fields")
+        return p, s
+
+    def powers(self):
+        a, b, c = C.c_double(), C.c_double(), C.c_double()
+        check(lib().shg_get_powers(self._h, C.byref(a), C.byref(b), C.byref(c)), "shg_get_powers")
+        return a.value, b.value, c.value
+
+    def efficiency(self) -> float:
+        e = C.c_double()
+        check(lib().shg_efficiency(self._h, C.byref(e)), "shg_efficiency")
+        return e.value
+
+
+class Sweep:
+    """Independent plain solves run together (one device schedule, CUDA graph)."""
+
+    def __init__(self, instances, crystal=None, device=0):
+        self.cfg = _cfg_from(crystal, device=device)
+        n = len(instances)
+        arr = (_lib.Instance * n)()
+        for k, it in enumerate(instances):
+            arr[k] = _lib.Instance(it.nx, it.ny, it.nz, it.lx, it.ly, it.power, it.waist, it.temp, it.focal)
+        self._arr = arr
+        self.instances = list(instances)
+        b = C.c_void_p()
+        check(lib().shg_batch_create(C.byref(self.cfg), arr, n, C.byref(b)), "shg_batch_create")
+        self._b = b
+        self.n = n
+
+    def close(self):
+        if getattr(self, "_b", None):
+            lib().shg_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, with_fields=False):
+        eta = np.zeros(self.n, np.float64)
+        fields = None
+        ptrs = None
+        if with_fields:
+            fields = [np.zeros((it.ny, it.nx), np.complex64) for it in self.instances]
+            ptrs = (C.POINTER(C.c_float) * self.n)(*[_pf(f) for f in fields])
+        check(lib().shg_batch_run(self._b, eta.ctypes.data_as(C.POINTER(C.c_double)), ptrs), "shg_batch_run")
+        return (eta, fields) if with_fields else eta
+
+    def run_async(self, stream):
+        check(lib().shg_batch_run_async(self._b, stream), "shg_batch_run_async")
+
+    def results(self):
+        eta = np.zeros(self.n, np.float64)
+        check(lib().shg_batch_results(self._b, eta.ctypes.data_as(C.POINTER(C.c_double))), "shg_batch_results")
+        return eta
+
+    def launch_count(self) -> int:
+        v = C.c_int()
+        check(lib().shg_batch_launch_count(self._b, C.byref(v)), "shg_batch_launch_count")
+        return v.value
+
+
+def dft2d_device(x, sign: int, out=None, stream=None):
+    """Unnormalised 2D DFT of a square (n, n) complex64 CUDA tensor (FFTW sign convention)."""
+    import torch
+    if out is None:
+        out = torch.empty_like(x)
+    st = torch.cuda.current_stream(x.device).cuda_stream if stream is None else stream
+    check(lib().shg_dft2d_device(x.shape[0], sign, x.data_ptr(), out.data_ptr(), st), "shg_dft2d_device")
+    return out

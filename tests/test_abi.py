@@ -1,0 +1,59 @@
+"""The C-ABI library loads without a GPU and exports every entry point of include/shg.h."""
+import os
+import re
+
+import pytest
+
+from _util import ROOT
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "shg.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(shg_\w+)\s*\(", src, flags=re.M)))
+
+
+def test_header_declares_entry_points():
+    names = _declared()
+    assert "shg_run" in names and "shg_batch_run" in names and len(names) >= 15
+
+
+def test_library_exports_all_declared_symbols():
+    from shg_focused_gaussian_beams_gb300 import _lib
+    L = _lib.lib()
+    missing = [n for n in _declared() if not hasattr(L, n)]
+    assert not missing, missing
+    # the Python binding covers every declared symbol
+    assert set(_declared()) <= set(_lib.SIGNATURES), set(_declared()) - set(_lib.SIGNATURES)
+
+
+def test_config_defaults_are_the_reference_constants():
+    """SHG.cpp:11-13 and Crystal.h:31-53 (no CUDA call involved)."""
+    from shg_focused_gaussian_beams_gb300 import _lib
+    c = _lib.default_config()
+    assert (c.nx, c.ny, c.nz) == (64, 64, 200)
+    assert (c.lx, c.ly, c.lz) == (2000.0, 1000.0, 30000.0)
+    import numpy as np
+    f = np.float32
+    assert f(c.deff) == f(11.00e-6) and f(c.lambda_qpm) == f(7.97) and f(c.alpha_p) == f(0.17e-6)
+    assert f(c.alpha_s) == f(1.57e-6) and f(c.beta_s) == f(5e-5) and f(c.kth) == f(8.4e-6)
+    assert f(c.htc) == f(10e-12) and c.thermal == 0 and c.sh_seed < 0
+
+
+def test_invalid_arguments_fail_loudly_without_gpu():
+    from shg_focused_gaussian_beams_gb300 import _lib
+    import ctypes as C
+    L = _lib.lib()
+    assert L.shg_config_init(None) == 1
+    assert L.shg_create(None, None) == 1
+    assert L.shg_batch_create(None, None, 0, None) == 1
+    assert b"null" in L.shg_last_error()
+
+
+def test_python_sellmeier_matches_oracle():
+    import numpy as np
+    import oracle as O
+    from shg_focused_gaussian_beams_gb300.workloads import sellmeier_n
+    for T in np.linspace(10, 90, 41, dtype=np.float32):
+        for L in (1.064, np.float32(0.532), 0.8):
+            assert sellmeier_n(L, T) == O.lib().oracle_n_f32(L, T)

@@ -1,0 +1,137 @@
+"""CUDA path against the oracle and the reference's golden outputs (GB300 only).
+
+Tolerance (stated bar): output fields within relative L2 1e-4 and conversion efficiency
+within 1e-4 relative, against the reference's FP32 build (golden fixtures and the
+bit-exact restatement) and against the FP64 run of the same method.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from _util import ETA_RTOL, FIELD_RTOL, cfg_from_golden, crystal_from_golden, eta, golden, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():  # pragma: no cover - CPU containers
+    pytest.skip("no CUDA device", allow_module_level=True)
+
+from shg_focused_gaussian_beams_gb300.solver import Solver, Sweep, dft2d_device  # noqa: E402
+from shg_focused_gaussian_beams_gb300 import workloads as W  # noqa: E402
+
+
+@pytest.mark.parametrize("n", [16, 32, 64, 128, 256])
+@pytest.mark.parametrize("sign", [-1, 1])
+def test_dft2d_vs_numpy(n, sign):
+    rng = np.random.default_rng(n + sign)
+    a = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))).astype(np.complex64)
+    ref = np.fft.fft2(a.astype(np.complex128)) if sign < 0 else np.fft.ifft2(a.astype(np.complex128)) * n * n
+    x = torch.from_numpy(a).cuda()
+    y = dft2d_device(x, sign)
+    torch.cuda.synchronize()
+    assert rel_l2(y.cpu().numpy(), ref) < 2e-6
+    # in place
+    dft2d_device(x, sign, out=x)
+    torch.cuda.synchronize()
+    assert rel_l2(x.cpu().numpy(), ref) < 2e-6
+
+
+def _solver_for(g):
+    return Solver(crystal=crystal_from_golden(g), nx=int(g["cfg_nx"]), ny=int(g["cfg_ny"]), nz=int(g["cfg_nz"]),
+                  lx=float(g["cfg_lx"]), ly=float(g["cfg_ly"]))
+
+
+@pytest.mark.parametrize("name", ["stock_plain.npz", "c0_small.npz", "c0_128x200.npz", "walkoff.npz"])
+def test_run_matches_reference_golden(name):
+    """Solver::run on the device (Gaussian pump and propagators built on the device)."""
+    g = golden(name)
+    s = _solver_for(g)
+    s.run(float(g["power"]), float(g["waist"]), float(g["focal"]), float(g["temp"]))
+    po, so = s.fields()
+    assert rel_l2(so, g["sh_out"]) < FIELD_RTOL
+    assert rel_l2(po, g["pump_out"]) < FIELD_RTOL
+    e_ref = eta(g["pump_in"], g["sh_out"], g["n_p"], g["n_s"])
+    assert abs(s.efficiency() - e_ref) / e_ref < ETA_RTOL
+
+
+@pytest.mark.parametrize("name", ["c0_small.npz", "stock_plain.npz"])
+def test_cwes_from_given_fields_matches_oracle(name):
+    """Arbitrary input fields (host API) against the bit-exact restatement."""
+    g = golden(name)
+    o = O.Oracle(cfg_from_golden(g))
+    temp = float(g["temp"])
+    rng = np.random.default_rng(5)
+    pump = g["pump_in"] * (1 + 0.05 * (rng.standard_normal(g["pump_in"].shape) +
+                                       1j * rng.standard_normal(g["pump_in"].shape)))
+    pump = pump.astype(np.complex64)
+    sh = (0.01 * pump * np.exp(1j * rng.uniform(0, 6.28, pump.shape))).astype(np.complex64)
+    po_r, so_r, _, _ = o.cwes_plain(pump, sh, temp)
+    s = _solver_for(g)
+    s.set_input_fields(pump, sh)
+    s.cwes(temp)
+    po, so = s.fields()
+    assert rel_l2(so, so_r) < FIELD_RTOL
+    assert rel_l2(po, po_r) < FIELD_RTOL
+
+
+def test_device_pointer_cwes_matches_host_api():
+    g = golden("c0_small.npz")
+    s = _solver_for(g)
+    temp = float(g["temp"])
+    s.set_input_fields(g["pump_in"])
+    s.cwes(temp)
+    po_h, so_h = s.fields()
+    p = torch.from_numpy(g["pump_in"]).cuda()
+    po_d, so_d = s.cwes_device(temp, p)
+    torch.cuda.synchronize()
+    assert np.array_equal(so_d.cpu().numpy(), so_h)
+    assert np.array_equal(po_d.cpu().numpy(), po_h)
+
+
+def test_fp64_parity_config_plain_128():
+    """Plain 128x128x200 workload: efficiency within 1e-4 of the FP64 run (FP32 delta-k)."""
+    g = golden("c0_128x200.npz")
+    o = O.Oracle(cfg_from_golden(g))
+    temp = float(g["temp"])
+    pump64 = o.set_pump64(float(g["power"]), float(g["focal"]), float(g["waist"]), temp)
+    _, so64, _, _ = o.cwes_plain64(pump64, np.zeros_like(pump64), temp, float(g["dk"]))
+    e64 = eta(pump64, so64, o.n64(1.064, temp), o.n64(0.532, temp))
+    s = _solver_for(g)
+    s.run(float(g["power"]), float(g["waist"]), float(g["focal"]), temp)
+    _, so = s.fields()
+    assert abs(s.efficiency() - e64) / e64 < ETA_RTOL
+    assert rel_l2(so, so64) < FIELD_RTOL
+
+
+def test_sweep_matches_oracle_and_single_solves():
+    insts = W.config_sweep(count=512, seed=2024)
+    # a spread of sizes and step counts, kept small enough for the CPU oracle
+    pick = [i for i in insts if i.nx <= 128 and i.nz <= 200][:10] + [i for i in insts if i.nx == 256][:2]
+    pick = [W.Instance(**{**i.as_dict(), "nz": min(i.nz, 100)}) for i in pick]
+    sw = Sweep(pick, crystal=W.CRYSTAL_QPM50)
+    eta_gpu, fields = sw.run(with_fields=True)
+    cfg = O.make_cfg(W.CRYSTAL_QPM50, 64, 64, 100)
+    eta_cpu = O.sweep_plain(cfg, pick, threads=8)
+    np.testing.assert_allclose(eta_gpu, eta_cpu, rtol=ETA_RTOL, atol=0)
+    # the batched result equals the single-solve path
+    k = 0
+    s = Solver(crystal=W.CRYSTAL_QPM50, nx=pick[k].nx, ny=pick[k].ny, nz=pick[k].nz, lx=pick[k].lx, ly=pick[k].ly)
+    s.run(pick[k].power, pick[k].waist, pick[k].focal, pick[k].temp)
+    _, so = s.fields()
+    assert rel_l2(fields[k], so) < 1e-6
+    # repeated runs (graph replay) give identical results
+    assert np.array_equal(sw.run(), eta_gpu)
+    assert sw.launch_count() > 0
+
+
+def test_errors_are_reported():
+    from shg_focused_gaussian_beams_gb300._lib import ShgError
+    with pytest.raises(ShgError, match="UNSUPPORTED"):
+        Solver(nx=48, ny=48, nz=10)
+    with pytest.raises(ShgError, match="UNSUPPORTED"):
+        Solver(nx=64, ny=32, nz=10)
+    s = Solver(nx=32, ny=32, nz=10)
+    with pytest.raises(ShgError, match="STATE"):
+        s.fields()
+    with pytest.raises(ShgError, match="STATE"):
+        s.cwes(50.0)

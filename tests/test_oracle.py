@@ -1,0 +1,126 @@
+"""The oracle restatement pinned against the reference's own outputs (CPU only).
+
+* Committed golden fixtures made by the reference build (tests/golden/make_golden.py):
+  bit-exact agreement of every component and of whole runs.
+* The reference build itself when present (development container): randomised
+  component comparisons, bit-exact.
+* The FFTW stand-in against numpy's FFT (double precision pocketfft).
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from _util import ETA_RTOL, FIELD_RTOL, bits_equal, cfg_from_golden, eta, golden, rel_l2
+import ref as R
+
+
+@pytest.mark.parametrize("name", ["stock_plain.npz", "c0_small.npz", "c0_128x200.npz", "walkoff.npz"])
+def test_plain_golden_bitexact(name):
+    g = golden(name)
+    o = O.Oracle(cfg_from_golden(g))
+    temp, power, waist, focal = (float(g[k]) for k in ("temp", "power", "waist", "focal"))
+    pump = o.set_pump(power, focal, waist, temp)
+    assert bits_equal(pump, g["pump_in"])
+    assert o.dk_constant(temp) == g["dk"]
+    assert o.n(1.064, temp) == g["n_p"]
+    if "hp" in g:
+        hp, hs = o.propagators(temp)
+        assert bits_equal(hp, g["hp"]) and bits_equal(hs, g["hs"])
+    po, so, _, _ = o.cwes_plain(pump, np.zeros_like(pump), temp)
+    assert bits_equal(po, g["pump_out"])
+    assert bits_equal(so, g["sh_out"])
+
+
+def test_stock_cli_matches_oracle():
+    """SHG.cpp's main as shipped starts the SH from clock-seeded N(0, 1e-20) noise; that
+    start is invisible at float precision in the output fields."""
+    g = golden("stock_cli.npz")
+    o = O.Oracle(cfg_from_golden(g))
+    P, w, T1, T2 = (float(v) for v in g["args"][:4])
+    po, so = o.run_plain(P, w, float(np.float32(0.5 * 30000.0)), T1)
+    assert rel_l2(so, g["sh_out"]) < 1e-6
+    assert rel_l2(po, g["pump_out"]) < 1e-6
+
+
+@pytest.mark.parametrize("name", ["thermal_topopen.npz", "thermal_oven.npz"])
+def test_thermal_golden_bitexact(name):
+    g = golden(name)
+    o = O.Oracle(cfg_from_golden(g))
+    bc = int(g["bc"])
+    T0 = o.init_temperature(float(g["temp"]), float(g["t1"]), float(g["t2"]), bc)
+    assert bits_equal(T0, g["T0"])
+    assert bits_equal(o.heat_sweeps(T0, g["Q"], 25.0, 37, bc), g["T37"])
+    assert bits_equal(o.dk_thermal(g["T"]), g["dk_T"])
+    res = o.thermal_run(float(g["power"]), float(g["waist"]), float(np.float32(0.5 * 30000.0)),
+                        float(g["temp"]), 25.0, float(g["t1"]), float(g["t2"]), bc=bc)
+    assert res["counts"] == list(g["counts"])
+    assert bits_equal(res["T"], g["T"])
+    assert bits_equal(res["sh"], g["sh_out"])
+    assert bits_equal(res["pump"], g["pump_out"])
+
+
+@pytest.mark.parametrize("n0,n1", [(64, 64), (128, 128), (32, 16), (48, 48), (12, 20)])
+@pytest.mark.parametrize("sign", [-1, 1])
+def test_dft_restatement_vs_numpy(n0, n1, sign):
+    rng = np.random.default_rng(n0 * 1000 + n1)
+    a = (rng.standard_normal((n0, n1)) + 1j * rng.standard_normal((n0, n1))).astype(np.complex64)
+    ref = np.fft.fft2(a.astype(np.complex128)) if sign < 0 else np.fft.ifft2(a.astype(np.complex128)) * (n0 * n1)
+    assert rel_l2(O.dft2d(a, sign), ref) < 2e-6
+    assert rel_l2(O.dft2d(a.astype(np.complex128), sign), ref) < 1e-13
+
+
+def test_dft_golden():
+    g = golden("dft64.npz")
+    assert bits_equal(O.dft2d(g["a"], -1), g["fwd"])
+    assert bits_equal(O.dft2d(g["a"], +1), g["bwd"])
+
+
+def test_fp64_oracle_agrees_with_fp32_given_dk():
+    """Same method in double with the reference's FP32 delta-k: efficiency and SH field
+    within the 1e-4 parity bar (measured here: 2.9e-5 and 1.5e-5, the FP32 FFT rounding
+    of 100 steps; with delta-k evaluated in double instead the gap is 3.5e-3)."""
+    g = golden("c0_small.npz")
+    o = O.Oracle(cfg_from_golden(g))
+    temp = float(g["temp"])
+    pump64 = o.set_pump64(float(g["power"]), float(g["focal"]), float(g["waist"]), temp)
+    _, so64, _, _ = o.cwes_plain64(pump64, np.zeros_like(pump64), temp, float(g["dk"]))
+    e32 = eta(g["pump_in"], g["sh_out"], g["n_p"], g["n_s"])
+    e64 = eta(pump64, so64, o.n64(1.064, temp), o.n64(0.532, temp))
+    assert abs(e64 - e32) / e32 < ETA_RTOL
+    assert rel_l2(so64, g["sh_out"]) < FIELD_RTOL
+
+
+@pytest.mark.skipif(not R.have("c0_small"), reason="reference build not present (development container only)")
+def test_oracle_vs_reference_build_random_inputs():
+    r = R.RefBuild("c0_small")
+    g = golden("c0_small.npz")
+    o = O.Oracle(cfg_from_golden(g))
+    rng = np.random.default_rng(3)
+    for temp in (48.7, 50.0, 51.3):
+        pump = r.set_pump(12.5, 15000.0, 31.0, temp)
+        pump = (pump * (1 + 0.05 * (rng.standard_normal(pump.shape) + 1j * rng.standard_normal(pump.shape)))).astype(np.complex64)
+        sh = (1e-3 * pump * rng.standard_normal(pump.shape)).astype(np.complex64)
+        a = r.cwes_plain(pump, sh, temp)
+        b = o.cwes_plain(pump, sh, temp)
+        for x, y in zip(a, b):
+            assert bits_equal(x, y)
+        pd, sd = r.diffraction(pump, sh, temp)
+        po, so = o.diffraction(pump, sh, temp)
+        assert bits_equal(pd, po) and bits_equal(sd, so)
+    for T in np.linspace(20.0, 80.0, 37, dtype=np.float32):
+        assert r.n(1.064, T) == o.n(1.064, T)
+        assert r.n(np.float32(0.532), T) == o.n(np.float32(0.532), T)
+
+
+@pytest.mark.skipif(not R.have("th_rect"), reason="reference build not present (development container only)")
+def test_oracle_vs_reference_build_thermal_rect():
+    import configs
+    c = configs.REF_BUILDS["th_rect"]
+    cfg = O.Cfg(c["nx"], c["ny"], c["nz"], c["lx"], c["ly"], c["lz"], c["lp"], c["deff"], c["lambda_qpm"],
+                c["alpha_p"], c["alpha_s"], c["beta_s"], c["rho_p"], c["rho_s"], c["kth"], c["htc"])
+    r, o = R.RefBuild("th_rect"), O.Oracle(cfg)
+    for bc in (0, 1):
+        a = r.thermal_run(25.0, 30.0, 15000.0, 49.0, 25.0, 49.5, 48.5, bc=bc)
+        b = o.thermal_run(25.0, 30.0, 15000.0, 49.0, 25.0, 49.5, 48.5, bc=bc)
+        assert a["counts"] == b["counts"]
+        assert bits_equal(a["T"], b["T"]) and bits_equal(a["sh"], b["sh"])
