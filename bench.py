@@ -1,0 +1,316 @@
+#!/usr/bin/env python
+"""Headline benchmark: grid-pt*z-steps/s of the batched SSFM sweep (and solves/s).
+
+Workload (default ``sweep``): 512 independent plain solves, seeded: pump power
+log-U(1, 50) W, focusing xi U(0.5, 5), oven 50 C +- 2 K, grid N^2 with N in {64, 128, 256},
+Nz in {100, 200, 400}, MgO:sPPLT crystal of the plain 128x128x200 workload, window 16 w0.
+One step = one pass of every solve (set-up + z-march + efficiency). Units: a solve of an
+N x N grid with Nz slices counts N*N*Nz grid-pt*z-steps (the reference's loop count,
+Solver.h:249), for both arms.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload sweep|plain128]
+
+--impl ours (default): ``value`` = device-resident throughput (instance table already on
+the GPU, CUDA events on the launching stream, K graph launches), ``e2e`` = the same
+through the public C ABI with host buffers (instance parameters uploaded and efficiencies
+plus all SH output fields read back every step), ``roofline`` from per-launch CUDA
+events of an instrumented run, ``cpu_baseline`` = the oracle restatement of the
+reference on a bounded sample on all host cores.
+--impl reference: the reference's CPU algorithm (the oracle restatement; the reference's
+own build needs sources absent on this machine) on all host cores, rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+from shg_focused_gaussian_beams_gb300 import workloads as W  # noqa: E402
+
+METRIC = "grid-pt·z-steps/s (batched SSFM sweep, 512 solves; solves/s alongside)"
+UNIT = "grid-pt·z-steps/s"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def pt_steps(insts):
+    return sum(i.nx * i.ny * i.nz for i in insts)
+
+
+def workload(name, rank=0):
+    if name == "sweep":
+        insts = W.config_sweep(count=512, seed=2024 + rank)
+        desc = {"workload": "sweep512: 512 plain solves, N in {64,128,256}, Nz in {100,200,400}, P log-U(1,50) W, "
+                            "xi U(0.5,5), T 50+-2 C, window 16 w0",
+                "solves": len(insts)}
+    elif name == "plain128":
+        insts = [W.config_plain_128()]
+        desc = {"workload": "plain 128x128x200, P=10 W, xi=2.84, 50 C, window 16 w0", "solves": 1}
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    desc["pt_steps_per_step"] = pt_steps(insts)
+    return insts, desc
+
+
+def cpu_sample(insts, cores):
+    """Bounded CPU sample: one solve per core from the workload, N <= 128 and Nz <= 200
+    (the CPU's per-point cost grows with N, so this flatters the CPU)."""
+    pick = [i for i in insts if i.nx <= 128 and i.nz <= 200][:max(1, cores)]
+    return pick or insts[:1]
+
+
+def oracle_rate(sample, cores, reps=1):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    cfg = O.make_cfg(W.CRYSTAL_QPM50, 64, 64, 100)
+    O.sweep_plain(cfg, sample[:1], threads=1)  # load / warm
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        O.sweep_plain(cfg, sample, threads=cores)
+        times.append(time.perf_counter() - t0)
+    return pt_steps(sample) / statistics.median(times), times
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+            t0 = time.time()
+            while not self.rows and time.time() - t0 < 3.0:  # sampler running before timing starts
+                time.sleep(0.05)
+            self.rows.clear()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if len(r) > 5 + k and r[5 + k] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic(kernel):
+    """DRAM bytes per grid point of one launch of `kernel` from the committed ncu summary
+    (profiles/ncu_traffic.json), or None."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f).get(kernel)
+    except (OSError, ValueError):
+        return None
+
+
+def dist_setup(n_gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(world, v):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    insts, desc = workload(args.workload)
+    cores = os.cpu_count() or 1
+    sample = cpu_sample(insts, cores) if args.workload == "sweep" else insts
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    cfg = O.make_cfg(W.CRYSTAL_QPM50, 64, 64, 100)
+    for _ in range(args.warmup):
+        O.sweep_plain(cfg, sample[:1], threads=1)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.sweep_plain(cfg, sample, threads=cores)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = pt_steps(sample) * args.steps / total
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": desc | {"sample_solves": len(sample)},
+            "solves_per_s": len(sample) * args.steps / total,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{len(sample)} solves of the workload (N<=128, Nz<=200) per step on "
+                                       f"{cores} threads; oracle restatement of the reference, FP32"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    from shg_focused_gaussian_beams_gb300.solver import Sweep
+
+    world, rank, local = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    insts, desc = workload(args.workload, rank)
+    sw = Sweep(insts, crystal=W.CRYSTAL_QPM50, device=local)
+    stream = torch.cuda.Stream()
+    for _ in range(max(args.warmup, 3)):
+        sw.run_async(stream.cuda_stream)
+    stream.synchronize()
+    launches = sw.launch_count()
+
+    # device-resident timed region
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            sw.run_async(stream.cuda_stream)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    ms = allmax(world, ev0.elapsed_time(ev1))
+    work = desc["pt_steps_per_step"]
+    value = work * world * args.steps / (ms * 1e-3)
+    solves_s = len(insts) * world * args.steps / (ms * 1e-3)
+    eta = sw.results()
+
+    # end to end through the C ABI: parameters in (pinned), efficiencies + SH fields out (pinned)
+    off = sw.field_offsets()
+    eta_h = torch.empty(len(insts), dtype=torch.float64, pin_memory=True)
+    fld_h = torch.empty(int(off[-1]) * 2, dtype=torch.float32, pin_memory=True)
+    eta_np = eta_h.numpy()
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sw.set_instances(insts)
+        sw.run(eta_out=eta_np, sh_out_all=fld_h.data_ptr())
+    torch.cuda.synchronize()
+    e2e_s = allmax(world, time.perf_counter() - t0)
+    h2d, d2h_fields = sw.io_bytes()
+    e2e = {"value": work * world * args.steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": len(insts) * 8 + d2h_fields,
+           "solves_per_s": len(insts) * world * args.steps / e2e_s}
+
+    # roofline of the dominant kernel from an instrumented run (per-launch CUDA events)
+    prof = sw.profile()
+    dom = max(prof, key=lambda k: prof[k][1])
+    n_l, ms_k, bytes_k = prof[dom]
+    peak, peak_kind = measured_hbm()
+    achieved = bytes_k / (ms_k * 1e-3) / 1e9
+    tr = ncu_traffic(dom)
+    pts_per_launch = bytes_k / n_l / (32.0 if dom.startswith("rows") else 48.0)
+    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind, "launches": n_l,
+            "ms_per_launch": ms_k / n_l, "algorithmic_bytes_per_launch": bytes_k / n_l,
+            "traffic": None if tr is None else tr * pts_per_launch,
+            "share_of_step": ms_k / sum(v[1] for v in prof.values()),
+            "kernels": {k: {"launches": v[0], "ms": v[1], "GBps": v[2] / (v[1] * 1e-3) / 1e9} for k, v in prof.items()}}
+
+    if rank == 0:
+        cores = os.cpu_count() or 1
+        sample = cpu_sample(insts, cores) if args.workload == "sweep" else insts
+        cpu_value, cpu_times = oracle_rate(sample, cores, reps=2)
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": desc | {"l2": "inputs larger than L2 (fields + propagators of 512 solves ~0.7 GB resident)",
+                                  "parallelism": f"dp{world} (independent solves per GPU)",
+                                  "crystal": "MgO:sPPLT, L=30 mm, QPM at 50 C, d_eff 6.75 pm/V"},
+                "solves_per_s": solves_s, "e2e": e2e, "gpu_launches": launches * args.steps,
+                "roofline": roof, "clocks": clk.summary(),
+                "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": cores, "kind": "port",
+                                 "sample": f"{len(sample)} solves of the workload (N<=128, Nz<=200) on {cores} "
+                                           f"threads, median of {len(cpu_times)} runs; oracle restatement, FP32"},
+                "eta_mean": float(np.mean(eta))}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["sweep", "plain128"], default="sweep")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

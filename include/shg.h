@@ -94,15 +94,36 @@ typedef struct shg_batch shg_batch;
  * window fields are ignored. */
 int shg_batch_create(const shg_config *crystal, const shg_instance *inst, int n, shg_batch **out);
 int shg_batch_destroy(shg_batch *b);
-/* Runs every solve and copies the efficiencies (n doubles) to the host; when fields_out
- * is not NULL, fields_out[i] receives the SH output field of solve i (NX*NY complex). */
-int shg_batch_run(shg_batch *b, double *eta, float **fields_out);
+/* Runs every solve and copies the efficiencies (n doubles) to the host; when sh_out_all
+ * is not NULL it receives the SH output fields of all solves back to back in solve order
+ * (solve i at the complex offset given by shg_batch_field_offsets). */
+int shg_batch_run(shg_batch *b, double *eta, float *sh_out_all);
+/* Replaces the run parameters of every solve (grids must stay the same); the next run
+ * uploads them. */
+int shg_batch_set_instances(shg_batch *b, const shg_instance *inst, int n);
+/* offsets[0..n]: complex offset of each solve's field in the contiguous output; offsets[n]
+ * is the total. */
+int shg_batch_field_offsets(shg_batch *b, long long *offsets);
 /* Device-only run on `stream` (results stay on the device); shg_batch_results copies the
  * efficiencies after the stream has been synchronised. */
 int shg_batch_run_async(shg_batch *b, void *stream);
 int shg_batch_results(shg_batch *b, double *eta);
+/* Bytes one re-parameterised run moves: parameters and device descriptors uploaded,
+ * and the SH output fields of all solves. */
+int shg_batch_io_bytes(shg_batch *b, long long *h2d_per_run, long long *d2h_fields);
 /* Number of kernel launches one run issues. */
 int shg_batch_launch_count(shg_batch *b, int *launches);
+
+/* Per-kernel timing of one un-captured run: CUDA events around every launch, summed per
+ * kernel (name like "rows<128>"), with the algorithmic bytes those launches must move
+ * (fields read and written once; propagators read once in the column pass). */
+typedef struct shg_kernel_stat {
+    char name[32];
+    int launches;
+    double ms;
+    double bytes;
+} shg_kernel_stat;
+int shg_batch_profile(shg_batch *b, shg_kernel_stat *stats, int max_stats, int *n_stats);
 
 /* ---- Components, for tests ------------------------------------------------------- */
 /* Unnormalised 2D DFT of an n x n complex array on the device (sign -1 forward, +1

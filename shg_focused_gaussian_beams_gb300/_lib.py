@@ -32,6 +32,10 @@ class Config(C.Structure):
                 ("sh_seed", _i), ("device", _i)]
 
 
+class KernelStat(C.Structure):
+    _fields_ = [("name", C.c_char * 32), ("launches", _i), ("ms", _d), ("bytes", _d)]
+
+
 class Instance(C.Structure):
     _fields_ = [("nx", _i), ("ny", _i), ("nz", _i), ("lx", _f), ("ly", _f), ("power", _f), ("waist", _f),
                 ("temp", _f), ("focal", _f)]
@@ -53,10 +57,14 @@ SIGNATURES = {
     "shg_last_error": (C.c_char_p, []),
     "shg_batch_create": (_i, [C.POINTER(Config), C.POINTER(Instance), _i, C.POINTER(_vp)]),
     "shg_batch_destroy": (_i, [_vp]),
-    "shg_batch_run": (_i, [_vp, _pd, C.POINTER(_pf)]),
+    "shg_batch_run": (_i, [_vp, _pd, _vp]),
+    "shg_batch_set_instances": (_i, [_vp, C.POINTER(Instance), _i]),
+    "shg_batch_field_offsets": (_i, [_vp, C.POINTER(C.c_longlong)]),
+    "shg_batch_profile": (_i, [_vp, C.POINTER(KernelStat), _i, _pi]),
     "shg_batch_run_async": (_i, [_vp, _vp]),
     "shg_batch_results": (_i, [_vp, _pd]),
     "shg_batch_launch_count": (_i, [_vp, _pi]),
+    "shg_batch_io_bytes": (_i, [_vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "shg_dft2d_device": (_i, [_i, _i, _vp, _vp, _vp]),
 }
 

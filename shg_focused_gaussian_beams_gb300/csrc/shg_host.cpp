@@ -26,6 +26,12 @@ thread_local std::string g_last_error;
 
 void set_error(const std::string &msg) { g_last_error = msg; }
 
+#define SHG_TRY_INT(expr)    \
+    do {                     \
+        int rc_ = (expr);    \
+        if (rc_) return rc_; \
+    } while (0)
+
 #define SHG_CUDA(call)                                                                                 \
     do {                                                                                               \
         cudaError_t e_ = (call);                                                                       \
@@ -180,18 +186,23 @@ class Batch {
         SHG_CUDA(cudaSetDevice(crystal.device));
         int rc = ensure_twiddles(crystal.device);
         if (rc) return rc;
-        // Memory plan: per solve P, S, Pout, Sout, Hp, Hs (n*n float2 each), stepc (nz
-        // float4), acc (4 doubles); every block 256-byte aligned.
+        // Memory plan: six regions (P, S, Pout, Sout, Hp, Hs), each holding the n*n complex
+        // points of every solve back to back in solve order (so a region is one contiguous
+        // copy), then the per-slice constants (nz float4 per solve) and the sums (4 doubles
+        // per solve). Each solve's block is a multiple of 2 KiB, so every pointer stays
+        // 256-byte aligned.
         auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-        size_t total = 0;
-        std::vector<size_t> off(n);
+        foff_.assign(n + 1, 0);
+        size_t nz_total = 0;
         for (int i = 0; i < n; ++i) {
-            off[i] = total;
-            const size_t nn = (size_t)sp[i].n * sp[i].n;
-            total += 6 * al(nn * sizeof(float2)) + al(sp[i].nz * sizeof(float4));
+            foff_[i + 1] = foff_[i] + (size_t)sp[i].n * sp[i].n;
+            nz_total += (size_t)sp[i].nz;
         }
-        const size_t acc_off = total;
-        total += al(4 * sizeof(double) * n);
+        const size_t pts = foff_[n];
+        const size_t region = al(pts * sizeof(float2));
+        const size_t step_off = 6 * region;
+        const size_t acc_off = step_off + al(nz_total * sizeof(float4));
+        const size_t total = acc_off + al(4 * sizeof(double) * n);
         SHG_CUDA(cudaMalloc(&pool_, total));
         pool_bytes_ = total;
         acc_ = reinterpret_cast<double *>(pool_ + acc_off);
@@ -200,23 +211,26 @@ class Batch {
         s_src_.assign(n, nullptr);
         max_nn_ = 0;
         max_nz_ = 0;
+        size_t zoff = 0;
         for (int i = 0; i < n; ++i) {
             InstDesc &d = desc_[i];
             std::memset(&d, 0, sizeof(d));
-            const size_t nn = (size_t)sp[i].n * sp[i].n, fb = al(nn * sizeof(float2));
-            char *p = pool_ + off[i];
-            d.P = reinterpret_cast<float2 *>(p);
-            d.S = reinterpret_cast<float2 *>(p + fb);
-            d.Pout = reinterpret_cast<float2 *>(p + 2 * fb);
-            d.Sout = reinterpret_cast<float2 *>(p + 3 * fb);
-            d.Hp = reinterpret_cast<float2 *>(p + 4 * fb);
-            d.Hs = reinterpret_cast<float2 *>(p + 5 * fb);
-            d.stepc = reinterpret_cast<float4 *>(p + 6 * fb);
+            const size_t nn = (size_t)sp[i].n * sp[i].n;
+            auto reg = [&](int r) { return reinterpret_cast<float2 *>(pool_ + r * region) + foff_[i]; };
+            d.P = reg(0);
+            d.S = reg(1);
+            d.Pout = reg(2);
+            d.Sout = reg(3);
+            d.Hp = reg(4);
+            d.Hs = reg(5);
+            d.stepc = reinterpret_cast<float4 *>(pool_ + step_off) + zoff;
+            zoff += (size_t)sp[i].nz;
             d.acc = acc_ + 4 * i;
             fill_scalars(cr_, sp[i], d);
             max_nn_ = std::max(max_nn_, (int)nn);
             max_nz_ = std::max(max_nz_, sp[i].nz);
         }
+        sout_all_ = desc_[0].Sout;
         SHG_CUDA(cudaMalloc(&d_desc_, n * sizeof(InstDesc)));
         // Size classes, each sorted by step count (descending) so that the solves still
         // marching at stage s form a prefix of the class list.
@@ -254,8 +268,7 @@ class Batch {
         const int keep_given = desc_[i].pump_given;
         fill_scalars(cr_, sp, desc_[i]);
         desc_[i].pump_given = keep_given;
-        desc_dirty_ = true;
-        invalidate_graph();
+        desc_dirty_ = true;  // the graph reads descriptors from device memory: no re-capture
         return SHG_OK;
     }
 
@@ -284,10 +297,13 @@ class Batch {
         }
         if (!use_graph) return enqueue(st);
         if (!graph_exec_) {
+            // Capture on a private stream (the caller's may be the legacy default stream,
+            // which cannot be captured); the graph is then launched on the caller's stream.
+            if (!capture_stream_) SHG_CUDA(cudaStreamCreateWithFlags(&capture_stream_, cudaStreamNonBlocking));
             cudaGraph_t g = nullptr;
-            SHG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-            int rc = enqueue(st);
-            cudaError_t e = cudaStreamEndCapture(st, &g);
+            SHG_CUDA(cudaStreamBeginCapture(capture_stream_, cudaStreamCaptureModeThreadLocal));
+            int rc = enqueue(capture_stream_);
+            cudaError_t e = cudaStreamEndCapture(capture_stream_, &g);
             if (rc) {
                 if (g) cudaGraphDestroy(g);
                 return rc;
@@ -336,6 +352,10 @@ class Batch {
     }
 
     const InstDesc &desc(int i) const { return desc_[i]; }
+    // SH output fields of all solves, contiguous in solve order; offset of solve i in points.
+    const float2 *sout_all() const { return sout_all_; }
+    size_t field_offset(int i) const { return foff_[i]; }
+    size_t total_points() const { return foff_.back(); }
     int size() const { return (int)desc_.size(); }
     const SolveParams &params(int i) const { return sp_[i]; }
 
@@ -345,7 +365,47 @@ class Batch {
         std::vector<int> steps;  // descending
     };
 
-    int enqueue(cudaStream_t st) {
+   public:
+    // Per-launch timing of one un-captured run: events around every kernel launch.
+    struct Recorder {
+        struct Rec {
+            std::string name;
+            double bytes;
+            cudaEvent_t a, b;
+        };
+        std::vector<Rec> recs;
+        int begin(const std::string &name, double bytes, cudaStream_t st) {
+            Rec r{name, bytes, nullptr, nullptr};
+            SHG_CUDA(cudaEventCreate(&r.a));
+            SHG_CUDA(cudaEventCreate(&r.b));
+            SHG_CUDA(cudaEventRecord(r.a, st));
+            recs.push_back(r);
+            return SHG_OK;
+        }
+        int end(cudaStream_t st) {
+            SHG_CUDA(cudaEventRecord(recs.back().b, st));
+            return SHG_OK;
+        }
+        ~Recorder() {
+            for (auto &r : recs) {
+                if (r.a) cudaEventDestroy(r.a);
+                if (r.b) cudaEventDestroy(r.b);
+            }
+        }
+    };
+
+    int profile(cudaStream_t st, Recorder &rec) {
+        if (desc_dirty_) {
+            SHG_CUDA(cudaMemcpyAsync(d_desc_, desc_.data(), desc_.size() * sizeof(InstDesc), cudaMemcpyHostToDevice, st));
+            desc_dirty_ = false;
+        }
+        SHG_TRY_INT(enqueue(st, &rec));
+        SHG_CUDA(cudaStreamSynchronize(st));
+        return SHG_OK;
+    }
+
+   private:
+    int enqueue(cudaStream_t st, Recorder *rec = nullptr) {
         SHG_CUDA(cudaMemsetAsync(acc_, 0, 4 * sizeof(double) * desc_.size(), st));
         for (int i = 0; i < (int)desc_.size(); ++i) {
             const size_t bytes = (size_t)desc_[i].n * desc_[i].n * sizeof(float2);
@@ -355,15 +415,27 @@ class Batch {
             else
                 SHG_CUDA(cudaMemsetAsync(desc_[i].S, 0, bytes, st));
         }
+        if (rec) SHG_TRY_INT(rec->begin("setup", 24.0 * (double)total_points(), st));
         SHG_CUDA(launch_setup(d_desc_, (int)desc_.size(), max_nn_, max_nz_, st));
+        if (rec) SHG_TRY_INT(rec->end(st));
         for (const auto &k : classes_) {
             const int K = k.steps[0];
             const int *list = d_lists_ + k.offset;
+            const double nn = (double)k.n * k.n;
+            const std::string rn = "rows<" + std::to_string(k.n) + ">", cn = "cols<" + std::to_string(k.n) + ">";
             for (int s = 0; s <= K; ++s) {
                 // solves with nsteps >= s run the row pass, nsteps >= s + 1 the column pass
                 const int nr = count_at_least(k.steps, s), nc = count_at_least(k.steps, s + 1);
+                // algorithmic bytes: both fields read and written (rows), plus both
+                // propagators read (columns)
+                if (rec) SHG_TRY_INT(rec->begin(rn, 32.0 * nn * nr, st));
                 SHG_CUDA(launch_rows(k.n, d_desc_, list, nr, s, st));
-                if (nc > 0) SHG_CUDA(launch_cols(k.n, d_desc_, list, nc, st));
+                if (rec) SHG_TRY_INT(rec->end(st));
+                if (nc > 0) {
+                    if (rec) SHG_TRY_INT(rec->begin(cn, 48.0 * nn * nc, st));
+                    SHG_CUDA(launch_cols(k.n, d_desc_, list, nc, st));
+                    if (rec) SHG_TRY_INT(rec->end(st));
+                }
             }
         }
         return SHG_OK;
@@ -391,6 +463,8 @@ class Batch {
 
     void release() {
         invalidate_graph();
+        if (capture_stream_) cudaStreamDestroy(capture_stream_);
+        capture_stream_ = nullptr;
         if (pool_) cudaFree(pool_);
         if (d_desc_) cudaFree(d_desc_);
         if (d_lists_) cudaFree(d_lists_);
@@ -402,6 +476,8 @@ class Batch {
     shg_config cr_{};
     std::vector<SolveParams> sp_;
     std::vector<InstDesc> desc_;
+    std::vector<size_t> foff_;
+    const float2 *sout_all_ = nullptr;
     std::vector<const float2 *> p_src_, s_src_;
     std::vector<Class> classes_;
     char *pool_ = nullptr;
@@ -412,6 +488,7 @@ class Batch {
     int max_nn_ = 0, max_nz_ = 0;
     bool desc_dirty_ = true;
     cudaGraphExec_t graph_exec_ = nullptr;
+    cudaStream_t capture_stream_ = nullptr;
 };
 
 int validate_config(const shg_config &c) {
@@ -765,24 +842,84 @@ int shg_batch_results(shg_batch *b, double *eta) {
     return SHG_OK;
 }
 
-int shg_batch_run(shg_batch *b, double *eta, float **fields_out) {
+int shg_batch_run(shg_batch *b, double *eta, float *sh_out_all) {
     if (!b) {
         set_error("null batch");
         return SHG_ERR_INVALID;
     }
     SHG_TRY(b->batch.run_async(b->stream, true));
     b->ran = true;
+    if (sh_out_all)
+        SHG_CUDA(cudaMemcpyAsync(sh_out_all, b->batch.sout_all(), b->batch.total_points() * sizeof(float2),
+                                 cudaMemcpyDeviceToHost, b->stream));
     SHG_CUDA(cudaStreamSynchronize(b->stream));
     if (eta) SHG_TRY(shg_batch_results(b, eta));
-    if (fields_out) {
-        for (int i = 0; i < b->batch.size(); ++i) {
-            if (!fields_out[i]) continue;
-            const InstDesc &d = b->batch.desc(i);
-            SHG_CUDA(cudaMemcpyAsync(fields_out[i], d.Sout, (size_t)d.n * d.n * sizeof(float2),
-                                     cudaMemcpyDeviceToHost, b->stream));
-        }
-        SHG_CUDA(cudaStreamSynchronize(b->stream));
+    return SHG_OK;
+}
+
+int shg_batch_set_instances(shg_batch *b, const shg_instance *inst, int n) {
+    if (!b || !inst || n != b->batch.size()) {
+        set_error("shg_batch_set_instances: null argument or solve count differs from the batch");
+        return SHG_ERR_INVALID;
     }
+    for (int i = 0; i < n; ++i) {
+        const shg_instance &s = inst[i];
+        SHG_TRY(b->batch.set_params(i, SolveParams{s.nx, s.nz, s.lx, s.ly, s.power, s.waist, s.focal, s.temp,
+                                                   s.temp, s.temp}));
+    }
+    return SHG_OK;
+}
+
+int shg_batch_field_offsets(shg_batch *b, long long *offsets) {
+    if (!b || !offsets) {
+        set_error("null argument");
+        return SHG_ERR_INVALID;
+    }
+    for (int i = 0; i <= b->batch.size(); ++i)
+        offsets[i] = (long long)(i < b->batch.size() ? b->batch.field_offset(i) : b->batch.total_points());
+    return SHG_OK;
+}
+
+int shg_batch_profile(shg_batch *b, shg_kernel_stat *stats, int max_stats, int *n_stats) {
+    if (!b || !stats || !n_stats || max_stats <= 0) {
+        set_error("null argument");
+        return SHG_ERR_INVALID;
+    }
+    Batch::Recorder rec;
+    SHG_TRY(b->batch.profile(b->stream, rec));
+    std::vector<std::string> order;
+    std::map<std::string, shg_kernel_stat> acc;
+    for (const auto &r : rec.recs) {
+        float ms = 0.f;
+        SHG_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
+        auto it = acc.find(r.name);
+        if (it == acc.end()) {
+            shg_kernel_stat z;
+            std::memset(&z, 0, sizeof(z));
+            std::snprintf(z.name, sizeof(z.name), "%s", r.name.c_str());
+            it = acc.emplace(r.name, z).first;
+            order.push_back(r.name);
+        }
+        it->second.launches += 1;
+        it->second.ms += ms;
+        it->second.bytes += r.bytes;
+    }
+    *n_stats = 0;
+    for (const auto &nm : order) {
+        if (*n_stats >= max_stats) break;
+        stats[(*n_stats)++] = acc[nm];
+    }
+    b->ran = true;
+    return SHG_OK;
+}
+
+int shg_batch_io_bytes(shg_batch *b, long long *h2d_per_run, long long *d2h_fields) {
+    if (!b) {
+        set_error("null batch");
+        return SHG_ERR_INVALID;
+    }
+    if (h2d_per_run) *h2d_per_run = (long long)(b->batch.size() * (sizeof(shg_instance) + sizeof(InstDesc)));
+    if (d2h_fields) *d2h_fields = (long long)(b->batch.total_points() * sizeof(float2));
     return SHG_OK;
 }
 

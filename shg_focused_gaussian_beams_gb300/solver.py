@@ -147,15 +147,42 @@ class Sweep:
         except Exception:
             pass
 
-    def run(self, with_fields=False):
-        eta = np.zeros(self.n, np.float64)
-        fields = None
-        ptrs = None
-        if with_fields:
-            fields = [np.zeros((it.ny, it.nx), np.complex64) for it in self.instances]
-            ptrs = (C.POINTER(C.c_float) * self.n)(*[_pf(f) for f in fields])
-        check(lib().shg_batch_run(self._b, eta.ctypes.data_as(C.POINTER(C.c_double)), ptrs), "shg_batch_run")
-        return (eta, fields) if with_fields else eta
+    def field_offsets(self):
+        off = np.zeros(self.n + 1, np.int64)
+        check(lib().shg_batch_field_offsets(self._b, off.ctypes.data_as(C.POINTER(C.c_longlong))),
+              "shg_batch_field_offsets")
+        return off
+
+    def run(self, with_fields=False, eta_out=None, sh_out_all=None):
+        """Run every solve. Returns efficiencies, and the SH output fields (list of (n, n)
+        complex64 views into one contiguous buffer) when with_fields is set.
+        eta_out / sh_out_all may be caller-owned (e.g. pinned) host buffers."""
+        eta = np.zeros(self.n, np.float64) if eta_out is None else eta_out
+        buf = sh_out_all
+        if with_fields and buf is None:
+            buf = np.zeros(int(self.field_offsets()[-1]), np.complex64)
+        ptr = None if buf is None else C.c_void_p(buf.ctypes.data if isinstance(buf, np.ndarray) else buf)
+        check(lib().shg_batch_run(self._b, eta.ctypes.data_as(C.POINTER(C.c_double)), ptr), "shg_batch_run")
+        if not with_fields:
+            return eta
+        off = self.field_offsets()
+        fields = [np.asarray(buf)[off[i]:off[i + 1]].reshape(it.ny, it.nx) for i, it in enumerate(self.instances)]
+        return eta, fields
+
+    def set_instances(self, instances):
+        arr = (_lib.Instance * self.n)()
+        for k, it in enumerate(instances):
+            arr[k] = _lib.Instance(it.nx, it.ny, it.nz, it.lx, it.ly, it.power, it.waist, it.temp, it.focal)
+        check(lib().shg_batch_set_instances(self._b, arr, self.n), "shg_batch_set_instances")
+        self._arr = arr
+        self.instances = list(instances)
+
+    def profile(self):
+        """Per-kernel totals of one instrumented run: {name: (launches, ms, algorithmic bytes)}."""
+        stats = (_lib.KernelStat * 64)()
+        n = C.c_int()
+        check(lib().shg_batch_profile(self._b, stats, 64, C.byref(n)), "shg_batch_profile")
+        return {stats[i].name.decode(): (stats[i].launches, stats[i].ms, stats[i].bytes) for i in range(n.value)}
 
     def run_async(self, stream):
         check(lib().shg_batch_run_async(self._b, stream), "shg_batch_run_async")
@@ -164,6 +191,12 @@ class Sweep:
         eta = np.zeros(self.n, np.float64)
         check(lib().shg_batch_results(self._b, eta.ctypes.data_as(C.POINTER(C.c_double))), "shg_batch_results")
         return eta
+
+    def io_bytes(self):
+        """(host->device bytes per re-parameterised run, device->host bytes of all SH fields)."""
+        a, b = C.c_longlong(), C.c_longlong()
+        check(lib().shg_batch_io_bytes(self._b, C.byref(a), C.byref(b)), "shg_batch_io_bytes")
+        return a.value, b.value
 
     def launch_count(self) -> int:
         v = C.c_int()

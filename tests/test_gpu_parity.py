@@ -119,8 +119,9 @@ def test_sweep_matches_oracle_and_single_solves():
     s.run(pick[k].power, pick[k].waist, pick[k].focal, pick[k].temp)
     _, so = s.fields()
     assert rel_l2(fields[k], so) < 1e-6
-    # repeated runs (graph replay) give identical results
-    assert np.array_equal(sw.run(), eta_gpu)
+    # repeated runs (graph replay) agree; the double-precision power sums are accumulated
+    # with atomics, so only their last bits may differ
+    np.testing.assert_allclose(sw.run(), eta_gpu, rtol=1e-12, atol=0)
     assert sw.launch_count() > 0
 
 
