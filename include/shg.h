@@ -56,8 +56,8 @@ int shg_destroy(shg_handle *h);
 /* Solver::run (Solver.h:279-355), same arguments in the same order. The output fields are
  * the state at the top of slice NZ-1 (what Solver::CWES saves as Pump_out/Signal_out,
  * Solver.h:250-255) and stay on the device until read. save_only_last / save_temperature
- * select the reference's text outputs when an output directory is set
- * (shg_set_output_dir); otherwise they are ignored. */
+ * are accepted for signature parity; the Files.h text outputs are written by the `shg`
+ * command line from the fields read back with shg_get_fields. */
 int shg_run(shg_handle *h, float power, float waist, float focalpoint, float temp, float t_inf,
             float t_peltier1, float t_peltier2, int save_only_last, int save_temperature);
 
