@@ -53,6 +53,10 @@ def workload(name, rank=0):
         desc = {"workload": "sweep512: 512 plain solves, N in {64,128,256}, Nz in {100,200,400}, P log-U(1,50) W, "
                             "xi U(0.5,5), T 50+-2 C, window 16 w0",
                 "solves": len(insts)}
+    elif name == "rows256":
+        # ncu-sized case: 64 solves of 256x256x100 (fields + propagators 200 MB > L2)
+        insts = [W.plain_instance(256, 100, 10.0, 2.84, 50.0) for _ in range(64)]
+        desc = {"workload": "64 plain solves 256x256x100 (profiling case)", "solves": len(insts)}
     elif name == "plain128":
         insts = [W.config_plain_128()]
         desc = {"workload": "plain 128x128x200, P=10 W, xi=2.84, 50 C, window 16 w0", "solves": 1}
@@ -304,7 +308,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["sweep", "plain128"], default="sweep")
+    ap.add_argument("--workload", choices=["sweep", "plain128", "rows256"], default="sweep")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

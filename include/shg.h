@@ -125,6 +125,20 @@ typedef struct shg_kernel_stat {
 } shg_kernel_stat;
 int shg_batch_profile(shg_batch *b, shg_kernel_stat *stats, int max_stats, int *n_stats);
 
+/* ---- Plain CWES without device allocation ---------------------------------------- */
+/* No counterpart in the reference. For callers that cannot call cudaMalloc (device memory
+ * owned up front by another allocator, allocation-free real-time loops, plugin hosts that
+ * forbid device allocation): the same plain CWES as shg_cwes_device, with every working
+ * buffer in one fixed file-scope device array instead of allocated memory. cfg gives the
+ * grid and crystal (NX = NY a power of two in [16, 128], NZ in [2, 4096]; larger sizes
+ * return SHG_ERR_INVALID); pump_in / sh_in (NULL: zero SH start) / pump_out / sh_out are
+ * caller-owned device buffers of NX*NY complex64; when eta is not NULL the call
+ * synchronises `stream` and stores the efficiency. The first call on a device, with that
+ * device current, does a one-time set-up (array address, twiddle tables); make it before
+ * any stream capture. All calls share the array: calls that overlap on the GPU race. */
+int shg_cwes_noalloc(const shg_config *cfg, float temp, const void *pump_in, const void *sh_in,
+                     void *pump_out, void *sh_out, double *eta, void *stream);
+
 /* ---- Components, for tests ------------------------------------------------------- */
 /* Unnormalised 2D DFT of an n x n complex array on the device (sign -1 forward, +1
  * backward, FFTW's convention), device pointers, in place allowed. */

@@ -66,6 +66,7 @@ SIGNATURES = {
     "shg_batch_launch_count": (_i, [_vp, _pi]),
     "shg_batch_io_bytes": (_i, [_vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "shg_dft2d_device": (_i, [_i, _i, _vp, _vp, _vp]),
+    "shg_cwes_noalloc": (_i, [C.POINTER(Config), _f, _vp, _vp, _vp, _vp, _pd, _vp]),
 }
 
 _lib = None

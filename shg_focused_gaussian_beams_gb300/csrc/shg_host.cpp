@@ -67,15 +67,6 @@ float sellmeier(float L, float T) {
     return (float)std::sqrt(n2);
 }
 
-struct SolveParams {
-    int n, nz;
-    float lx, ly;
-    float power, waist, focal;
-    float temp;   // coupling and phase-mismatch temperature (dAdz, initDKConstant)
-    float tpump;  // index temperature of the Gaussian pump (setPump reads T at the grid centre)
-    float tprop;  // index temperature of the propagators (beamPropagator, same centre value)
-};
-
 // Fill the scalar part of a descriptor (pointers are set by the caller).
 void fill_scalars(const shg_config &cr, const SolveParams &sp, InstDesc &d) {
     const Phys ph;

@@ -5,6 +5,8 @@
 
 #include <string>
 
+#include "../../include/shg.h"
+
 namespace shg {
 
 struct InstDesc;
@@ -19,7 +21,22 @@ cudaError_t launch_cols(int n, const InstDesc *inst, const int *list, int count,
 bool line_length_supported(int n);
 cudaError_t launch_dft2d(int n, int sign, const float2 *in, float2 *out, cudaStream_t st);
 
+// One solve's run parameters (Solver::run arguments and the temperatures its set-up
+// calls read).
+struct SolveParams {
+    int n, nz;
+    float lx, ly;
+    float power, waist, focal;
+    float temp;   // coupling and phase-mismatch temperature (dAdz, initDKConstant)
+    float tpump;  // index temperature of the Gaussian pump (setPump reads T at the grid centre)
+    float tprop;  // index temperature of the propagators (beamPropagator, same centre value)
+};
+
 // shg_host.cpp
 void set_error(const std::string &msg);
+float sellmeier(float L, float T);
+void fill_scalars(const shg_config &cr, const SolveParams &sp, InstDesc &d);
+double field_power(double sum_abs2, float n_index, float dx, float dy);
+int ensure_twiddles(int device);
 
 }  // namespace shg
