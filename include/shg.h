@@ -82,6 +82,20 @@ int shg_efficiency(shg_handle *h, double *eta);
 
 const char *shg_last_error(void);
 
+/* ---- THERMAL (cfg.thermal = 1) ----------------------------------------------------- */
+/* After shg_run on a thermal handle: the final temperature tensor (NX*NY*NZ floats,
+ * Tfield::Tfinal) and the Jacobi sweep count of each of the five outer iterations of
+ * Solver.h:295-338 (-1 for iterations not run). */
+int shg_get_temperature(shg_handle *h, float *T);
+int shg_get_jacobi_counts(shg_handle *h, int *counts5);
+/* Components on host buffers (NX = NY; grid from cfg): Tfield.h:31-110 initial
+ * temperature; `nsweeps` sweeps of Tfield.h:113 (bc 0) or Tfield.h:224 (bc 1), each followed
+ * by Tinic <- Tfinal (Solver.h:321), T updated in place, Q the heat source; and
+ * PhaseMatching.h:41-54 delta-k(T) with the two refractive indices (any output may be NULL). */
+int shg_init_temperature(const shg_config *cfg, float temp, float t1, float t2, int bc, float *T_out);
+int shg_heat_sweeps(const shg_config *cfg, float *T_inout, const float *Q, float t_inf, int nsweeps, int bc);
+int shg_dk_thermal(const shg_config *cfg, const float *T, float *DK, float *NP, float *NS);
+
 /* ---- Batched sweep: many independent plain solves in one device schedule ----------- */
 typedef struct shg_instance {
     int nx, ny, nz;          /* per-solve grid (square, power of two) */

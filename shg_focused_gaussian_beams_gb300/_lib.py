@@ -66,6 +66,11 @@ SIGNATURES = {
     "shg_batch_launch_count": (_i, [_vp, _pi]),
     "shg_batch_io_bytes": (_i, [_vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "shg_dft2d_device": (_i, [_i, _i, _vp, _vp, _vp]),
+    "shg_get_temperature": (_i, [_vp, _pf]),
+    "shg_get_jacobi_counts": (_i, [_vp, _pi]),
+    "shg_init_temperature": (_i, [C.POINTER(Config), _f, _f, _f, _i, _pf]),
+    "shg_heat_sweeps": (_i, [C.POINTER(Config), _pf, _pf, _f, _i, _i]),
+    "shg_dk_thermal": (_i, [C.POINTER(Config), _pf, _pf, _pf, _pf]),
     "shg_cwes_noalloc": (_i, [C.POINTER(Config), _f, _vp, _vp, _vp, _vp, _pd, _vp]),
 }
 

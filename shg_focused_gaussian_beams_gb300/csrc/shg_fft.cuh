@@ -27,6 +27,14 @@
 
 namespace shg {
 
+constexpr int kMaxLine = 256;
+
+// Twiddle tables exp(-2 pi i m / N) for N = 16..kMaxLine: the table for line length N
+// sits at [N, 2N). Each translation unit that launches line FFTs has its own copy
+// (internal linkage) and registers its address with twiddle_tables_register(); the host
+// fills every registered copy once per device.
+static __device__ float2 g_twiddle[2 * kMaxLine];
+
 __device__ __forceinline__ float2 c_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 c_sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ float2 c_mul(float2 a, float2 b) {

@@ -17,6 +17,9 @@
 #include "../../include/shg.h"
 #include "shg_internal.h"
 #include "shg_march.cuh"
+#include "shg_thermal_host.h"
+
+#include <memory>
 
 namespace shg {
 
@@ -139,12 +142,14 @@ int ensure_twiddles(int device) {
             const double a = 2.0 * 3.14159265358979323846264338327950288 * (double)m / (double)N;
             tab[N + m] = make_float2((float)std::cos(a), (float)(-std::sin(a)));
         }
-    void *p = const_cast<float2 *>(twiddle_symbol_address());
-    if (!p) {
-        set_error("twiddle table symbol unavailable");
-        return SHG_ERR_CUDA;
+    for (const float2 *addr : {twiddle_symbol_address_march(), twiddle_symbol_address_thermal()}) {
+        void *p = const_cast<float2 *>(addr);
+        if (!p) {
+            set_error("twiddle table symbol unavailable");
+            return SHG_ERR_CUDA;
+        }
+        SHG_CUDA(cudaMemcpy(p, tab.data(), tab.size() * sizeof(float2), cudaMemcpyHostToDevice));
     }
-    SHG_CUDA(cudaMemcpy(p, tab.data(), tab.size() * sizeof(float2), cudaMemcpyHostToDevice));
     done[device] = true;
     return SHG_OK;
 }
@@ -505,6 +510,7 @@ using namespace shg;
 struct shg_handle {
     shg_config cfg;
     Batch batch;
+    std::unique_ptr<ThermalSolve> th;  // set for thermal configurations
     SolveParams sp{};
     int n = 0;
     float2 *stage_p = nullptr, *stage_s = nullptr;  // device staging of given input fields
@@ -609,13 +615,24 @@ int shg_create(const shg_config *cfg, shg_handle **out) {
     }
     *out = nullptr;
     SHG_TRY(validate_config(*cfg));
-    if (cfg->thermal) {
-        set_error("THERMAL runs are not available in this build");
-        return SHG_ERR_UNSUPPORTED;
-    }
     auto *h = new shg_handle;
     h->cfg = *cfg;
     h->n = cfg->nx;
+    if (cfg->thermal) {
+        if (cfg->bc != 0 && cfg->bc != 1) {
+            delete h;
+            set_error("bc must be 0 (open top) or 1 (oven surrounded)");
+            return SHG_ERR_INVALID;
+        }
+        h->th.reset(new ThermalSolve);
+        int rc = h->th->create(*cfg);
+        if (rc) {
+            delete h;
+            return rc;
+        }
+        *out = h;
+        return SHG_OK;
+    }
     h->sp = SolveParams{cfg->nx, cfg->nz, cfg->lx, cfg->ly, 1.0f, 30.0f, 0.5f * cfg->lz, 50.0f, 50.0f, 50.0f};
     int rc = h->batch.create(*cfg, {h->sp});
     if (rc) {
@@ -640,6 +657,10 @@ int shg_destroy(shg_handle *h) {
 
 int shg_set_input_pump(shg_handle *h, float power, float focalpoint, float waist, float tc) {
     SHG_TRY(check_handle(h));
+    if (h->th) {
+        set_error("plain-path entry point called on a thermal handle");
+        return SHG_ERR_STATE;
+    }
     h->sp.power = power;
     h->sp.focal = focalpoint;
     h->sp.waist = waist;
@@ -651,6 +672,10 @@ int shg_set_input_pump(shg_handle *h, float power, float focalpoint, float waist
 
 int shg_set_input_fields(shg_handle *h, const float *pump, const float *sh) {
     SHG_TRY(check_handle(h));
+    if (h->th) {
+        set_error("plain-path entry point called on a thermal handle");
+        return SHG_ERR_STATE;
+    }
     if (!pump) {
         set_error("pump field required");
         return SHG_ERR_INVALID;
@@ -670,6 +695,10 @@ int shg_set_input_fields(shg_handle *h, const float *pump, const float *sh) {
 
 int shg_cwes(shg_handle *h, float temp) {
     SHG_TRY(check_handle(h));
+    if (h->th) {
+        set_error("plain-path entry point called on a thermal handle");
+        return SHG_ERR_STATE;
+    }
     if (!h->have_pump) {
         set_error("shg_cwes: no input pump (shg_set_input_pump or shg_set_input_fields first)");
         return SHG_ERR_STATE;
@@ -684,6 +713,10 @@ int shg_cwes(shg_handle *h, float temp) {
 int shg_cwes_device(shg_handle *h, float temp, const void *pump_in, const void *sh_in, void *pump_out,
                     void *sh_out, void *stream) {
     SHG_TRY(check_handle(h));
+    if (h->th) {
+        set_error("plain-path entry point called on a thermal handle");
+        return SHG_ERR_STATE;
+    }
     if (!pump_in) {
         set_error("pump_in required");
         return SHG_ERR_INVALID;
@@ -707,11 +740,13 @@ int shg_cwes_device(shg_handle *h, float temp, const void *pump_in, const void *
 int shg_run(shg_handle *h, float power, float waist, float focalpoint, float temp, float t_inf, float t_peltier1,
             float t_peltier2, int save_only_last, int save_temperature) {
     SHG_TRY(check_handle(h));
-    (void)t_inf;
-    (void)t_peltier1;
-    (void)t_peltier2;
     (void)save_only_last;
     (void)save_temperature;
+    if (h->th) {
+        SHG_TRY(h->th->run(power, waist, focalpoint, temp, t_inf, t_peltier1, t_peltier2));
+        h->have_result = true;
+        return SHG_OK;
+    }
     // Solver.h:342-348: pump, SH start, propagators and delta-k all at Temp.
     h->sp.power = power;
     h->sp.waist = waist;
@@ -740,6 +775,7 @@ int shg_get_fields(shg_handle *h, float *pump_out, float *sh_out) {
         set_error("no result yet");
         return SHG_ERR_STATE;
     }
+    if (h->th) return h->th->copy_fields(pump_out, sh_out);
     const InstDesc &d = h->batch.desc(0);
     const size_t bytes = (size_t)h->n * h->n * sizeof(float2);
     SHG_CUDA(cudaStreamSynchronize(h->stream));
@@ -754,6 +790,7 @@ int shg_get_powers(shg_handle *h, double *p_pump_in, double *p_sh_out, double *p
         set_error("no result yet");
         return SHG_ERR_STATE;
     }
+    if (h->th) return h->th->powers(p_pump_in, p_sh_out, p_pump_out);
     std::vector<double> acc;
     SHG_CUDA(cudaDeviceSynchronize());
     SHG_TRY(h->batch.copy_acc(acc));
@@ -769,6 +806,25 @@ int shg_efficiency(shg_handle *h, double *eta) {
         set_error("efficiency is not finite");
         return SHG_ERR_NONFINITE;
     }
+    return SHG_OK;
+}
+
+int shg_get_temperature(shg_handle *h, float *T) {
+    SHG_TRY(check_handle(h));
+    if (!h->th || !h->th->has_result() || !T) {
+        set_error("shg_get_temperature: needs a thermal handle after shg_run");
+        return SHG_ERR_STATE;
+    }
+    return h->th->copy_temperature(T);
+}
+
+int shg_get_jacobi_counts(shg_handle *h, int *counts) {
+    SHG_TRY(check_handle(h));
+    if (!h->th || !h->th->has_result() || !counts) {
+        set_error("shg_get_jacobi_counts: needs a thermal handle after shg_run");
+        return SHG_ERR_STATE;
+    }
+    h->th->counts(counts);
     return SHG_OK;
 }
 

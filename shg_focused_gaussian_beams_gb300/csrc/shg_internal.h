@@ -11,15 +11,28 @@ namespace shg {
 
 struct InstDesc;
 
-constexpr int kMaxLine = 256;
+// Device addresses of every translation unit's twiddle-table copy (current device).
+const float2 *twiddle_symbol_address_march();
+const float2 *twiddle_symbol_address_thermal();
 
 // shg_march.cu
-const float2 *twiddle_symbol_address();
 cudaError_t launch_setup(const InstDesc *inst, int n_inst, int max_nn, int max_nz, cudaStream_t st);
 cudaError_t launch_rows(int n, const InstDesc *inst, const int *list, int count, int s, cudaStream_t st);
 cudaError_t launch_cols(int n, const InstDesc *inst, const int *list, int count, cudaStream_t st);
 bool line_length_supported(int n);
 cudaError_t launch_dft2d(int n, int sign, const float2 *in, float2 *out, cudaStream_t st);
+
+// shg_thermal.cu
+struct HeatCoef;
+struct ThermDesc;
+cudaError_t launch_init_temperature(float *T, int nx, int ny, int nz, float temp, float t1, float t2, int bc,
+                                    cudaStream_t st);
+cudaError_t launch_heat(float *Tf, const float *Ti, const float *QK, const HeatCoef &c, int nx, int ny, int nz,
+                        int bc, cudaStream_t st);
+cudaError_t launch_sq_diff_sum(const float *Tf, const float *Ti, size_t n, double *out, cudaStream_t st);
+cudaError_t launch_sellmeier_tables(const float *T, float *NP, float *NS, float *DK, size_t n, float lp, float ls,
+                                    float two_pi, float inv_lambda, cudaStream_t st);
+cudaError_t launch_rows_th(int n, const InstDesc *d, const ThermDesc &th, int s, cudaStream_t st);
 
 // One solve's run parameters (Solver::run arguments and the temperatures its set-up
 // calls read).

@@ -22,10 +22,7 @@
 
 namespace shg {
 
-// Twiddle tables exp(-2 pi i m / N): the table for line length N sits at [N, 2N).
-__device__ float2 g_twiddle[2 * kMaxLine];
-
-const float2 *twiddle_symbol_address() {
+const float2 *twiddle_symbol_address_march() {
     void *p = nullptr;
     cudaGetSymbolAddress(&p, g_twiddle);
     return static_cast<const float2 *>(p);

@@ -1,0 +1,66 @@
+// Host orchestration of one THERMAL solve (Solver::run with -DTHERMAL, Solver.h:287-340).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "shg_internal.h"
+#include "shg_thermal.cuh"
+
+namespace shg {
+
+// Tfield.h:118-125 coefficients with the reference's rounding.
+HeatCoef make_heat_coef(const shg_config &cfg, float t_inf);
+
+class ThermalSolve {
+   public:
+    ~ThermalSolve();
+    int create(const shg_config &cfg);
+    // Solver::run (THERMAL): temperature set-up, then up to five outer iterations of
+    // {Jacobi to the reference's stop rule, delta-k(T), pump and propagators at the centre
+    // temperature, CWES with heat-source updates}.
+    int run(float power, float waist, float focal, float temp, float t_inf, float t1, float t2);
+    int copy_temperature(float *T_host);
+    int copy_fields(float *pump, float *sh);
+    void counts(int *c) const {
+        for (int i = 0; i < 5; ++i) c[i] = counts_[i];
+    }
+    int powers(double *pin, double *psh, double *pout);
+    bool has_result() const { return have_result_; }
+
+    // Components (device buffers owned here).
+    int jacobi(float t_inf, int *counter);   // one Jacobi solve with the reference's stop rule
+    int sweeps(float t_inf, int n);          // n plain sweeps
+    int cwes(float power, float waist, float focal);  // one thermal CWES from the current T
+
+    float *T_cur() { return T_[cur_]; }
+    float *T_prev() { return T_[cur_ ^ 1]; }
+    float *QK() { return qk_; }
+    size_t tsize() const { return tsize_; }
+    cudaStream_t stream() const { return st_; }
+
+   private:
+    int sq_diff(float *out);
+    shg_config cfg_{};
+    int n_ = 0, nz_ = 0, bc_ = 0;
+    size_t tsize_ = 0;
+    float *T_[2] = {nullptr, nullptr};
+    int cur_ = 0;
+    float *qk_ = nullptr, *np_ = nullptr, *ns_ = nullptr, *dk_ = nullptr, *dkint_ = nullptr;
+    float2 *f_ = nullptr;   // P, S, Pout, Sout, Hp, Hs
+    float4 *stepc_ = nullptr;
+    double *acc_ = nullptr, *scratch_sum_ = nullptr;
+    InstDesc *d_desc_ = nullptr;
+    InstDesc h_desc_{};
+    ThermDesc th_{};
+    HeatCoef hc_{};
+    float tinf_coef_ = -1e30f;
+    cudaStream_t st_ = nullptr;
+    int counts_[5] = {-1, -1, -1, -1, -1};
+    float tc_ = 0.f, temp_ = 0.f;
+    bool have_result_ = false;
+    int sh_seed_ = -1;
+};
+
+}  // namespace shg

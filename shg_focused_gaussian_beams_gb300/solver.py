@@ -119,6 +119,17 @@ class Solver:
         check(lib().shg_efficiency(self._h, C.byref(e)), "shg_efficiency")
         return e.value
 
+    # THERMAL results (Tfield::Tfinal and the Jacobi sweep counts of Solver.h:295-338)
+    def temperature(self):
+        T = np.zeros((self.nz, self.ny, self.nx), np.float32)
+        check(lib().shg_get_temperature(self._h, _pf(T)), "shg_get_temperature")
+        return T
+
+    def jacobi_counts(self):
+        c = (C.c_int * 5)()
+        check(lib().shg_get_jacobi_counts(self._h, c), "shg_get_jacobi_counts")
+        return list(c)
+
 
 class Sweep:
     """Independent plain solves run together (one device schedule, CUDA graph)."""
@@ -202,6 +213,43 @@ class Sweep:
         v = C.c_int()
         check(lib().shg_batch_launch_count(self._b, C.byref(v)), "shg_batch_launch_count")
         return v.value
+
+
+def _grid_cfg(crystal, nx, ny, nz, lx=None, ly=None):
+    kw = dict(nx=nx, ny=ny, nz=nz)
+    if lx is not None:
+        kw["lx"] = float(lx)
+    if ly is not None:
+        kw["ly"] = float(ly)
+    return _cfg_from(crystal, **kw)
+
+
+def init_temperature(crystal, nx, ny, nz, temp, t1, t2, bc, lx=None, ly=None):
+    """Tfield.h:31-110 on the device."""
+    cfg = _grid_cfg(crystal, nx, ny, nz, lx, ly)
+    T = np.zeros((nz, ny, nx), np.float32)
+    check(lib().shg_init_temperature(C.byref(cfg), temp, t1, t2, bc, _pf(T)), "shg_init_temperature")
+    return T
+
+
+def heat_sweeps(crystal, T, Q, t_inf, nsweeps, bc, lx=None, ly=None):
+    """`nsweeps` Jacobi sweeps of Tfield.h:113 (bc 0) / 224 (bc 1) on the device."""
+    nz, ny, nx = T.shape
+    cfg = _grid_cfg(crystal, nx, ny, nz, lx, ly)
+    Tn = np.ascontiguousarray(T, np.float32).copy()
+    Qn = np.ascontiguousarray(Q, np.float32)
+    check(lib().shg_heat_sweeps(C.byref(cfg), _pf(Tn), _pf(Qn), t_inf, nsweeps, bc), "shg_heat_sweeps")
+    return Tn
+
+
+def dk_thermal(crystal, T, lx=None, ly=None):
+    """PhaseMatching.h:41-54 on the device: (delta-k, n_p, n_s) per voxel."""
+    nz, ny, nx = T.shape
+    cfg = _grid_cfg(crystal, nx, ny, nz, lx, ly)
+    D, NP, NS = (np.zeros(T.shape, np.float32) for _ in range(3))
+    check(lib().shg_dk_thermal(C.byref(cfg), _pf(np.ascontiguousarray(T, np.float32)), _pf(D), _pf(NP), _pf(NS)),
+          "shg_dk_thermal")
+    return D, NP, NS
 
 
 def dft2d_device(x, sign: int, out=None, stream=None):

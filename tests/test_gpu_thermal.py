@@ -1,0 +1,88 @@
+"""THERMAL path on the device against the reference (GB300 only).
+
+The heat stencil, the initial temperature and delta-k(T) must be bit-identical to the
+reference's build (golden fixtures). A full THERMAL run must take the reference's
+Jacobi sweep counts and agree within the parity bar (fields 1e-4 relative L2, efficiency
+1e-4); its temperature differs only through the heat source, which depends on the fields.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from _util import ETA_RTOL, FIELD_RTOL, bits_equal, cfg_from_golden, crystal_from_golden, eta, golden, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():  # pragma: no cover - CPU containers
+    pytest.skip("no CUDA device", allow_module_level=True)
+
+from shg_focused_gaussian_beams_gb300 import solver as S  # noqa: E402
+from shg_focused_gaussian_beams_gb300 import workloads as W  # noqa: E402
+
+FOCAL = float(np.float32(0.5 * 30000.0))
+
+
+def _geom(g):
+    return dict(lx=float(g["cfg_lx"]), ly=float(g["cfg_ly"]))
+
+
+@pytest.mark.parametrize("name", ["thermal_topopen.npz", "thermal_oven.npz"])
+def test_heat_components_bitexact(name):
+    g = golden(name)
+    cr = crystal_from_golden(g)
+    nz, ny, nx = g["T0"].shape
+    bc = int(g["bc"])
+    T0 = S.init_temperature(cr, nx, ny, nz, float(g["temp"]), float(g["t1"]), float(g["t2"]), bc, **_geom(g))
+    assert bits_equal(T0, g["T0"])
+    T37 = S.heat_sweeps(cr, g["T0"], g["Q"], 25.0, 37, bc, **_geom(g))
+    assert bits_equal(T37, g["T37"])
+    D, NP, NS = S.dk_thermal(cr, g["T"], **_geom(g))
+    assert bits_equal(D, g["dk_T"])
+
+
+def test_heat_sweeps_bitexact_vs_oracle_random():
+    cfg = O.make_cfg(W.CRYSTAL_QPM50, 64, 64, 40, 900.0, 450.0)
+    o = O.Oracle(cfg)
+    rng = np.random.default_rng(4)
+    for bc in (0, 1):
+        T = o.init_temperature(47.0, 49.0, 45.5, bc)
+        T = (T + rng.normal(0, 0.01, T.shape)).astype(np.float32)
+        Q = (rng.random(T.shape) * 5e-9).astype(np.float32)
+        ref = o.heat_sweeps(T, Q, 25.0, 61, bc)
+        got = S.heat_sweeps(W.CRYSTAL_QPM50, T, Q, 25.0, 61, bc, lx=900.0, ly=450.0)
+        assert bits_equal(got, ref)
+    D, NP, NS = S.dk_thermal(W.CRYSTAL_QPM50, T, lx=900.0, ly=450.0)
+    assert bits_equal(D, o.dk_thermal(T))
+
+
+@pytest.mark.parametrize("name", ["thermal_topopen.npz", "thermal_oven.npz"])
+def test_thermal_run_matches_reference(name):
+    g = golden(name)
+    nz, ny, nx = g["T"].shape
+    s = S.Solver(crystal=crystal_from_golden(g), nx=nx, ny=ny, nz=nz, thermal=True, bc=int(g["bc"]), **_geom(g))
+    s.run(float(g["power"]), float(g["waist"]), FOCAL, float(g["temp"]), 25.0, float(g["t1"]), float(g["t2"]))
+    assert s.jacobi_counts() == list(g["counts"])
+    po, so = s.fields()
+    assert rel_l2(so, g["sh_out"]) < FIELD_RTOL
+    assert rel_l2(po, g["pump_out"]) < FIELD_RTOL
+    T = s.temperature()
+    assert np.max(np.abs(T - g["T"])) < 1e-4
+    o = O.Oracle(cfg_from_golden(g))
+    tc = float(g["T"][0, ny // 2, nx // 2])
+    pin = o.set_pump(float(g["power"]), FOCAL, float(g["waist"]), tc)
+    e_ref = eta(pin, g["sh_out"], o.n(1.064, tc), o.n(np.float32(0.532), tc))
+    assert abs(s.efficiency() - e_ref) / e_ref < ETA_RTOL
+
+
+def test_thermal_run_64_oven_vs_oracle():
+    """64x64x60 oven-surrounded run against the restatement (five outer iterations)."""
+    inst = W.plain_instance(64, 60, 25.0, 2.84, 51.0)
+    cfg = O.make_cfg(W.CRYSTAL_QPM50, 64, 64, 60, inst.lx, inst.ly)
+    ref = O.Oracle(cfg).thermal_run(25.0, inst.waist, FOCAL, 51.0, 25.0, 51.0, 51.0, bc=1)
+    s = S.Solver(crystal=W.CRYSTAL_QPM50, nx=64, ny=64, nz=60, lx=inst.lx, ly=inst.ly, thermal=True, bc=1)
+    s.run(25.0, inst.waist, FOCAL, 51.0, 25.0, 51.0, 51.0)
+    assert s.jacobi_counts() == ref["counts"]
+    po, so = s.fields()
+    assert rel_l2(so, ref["sh"]) < FIELD_RTOL
+    assert np.max(np.abs(s.temperature() - ref["T"])) < 1e-4
