@@ -66,6 +66,59 @@ def workload(name, rank=0):
     return insts, desc
 
 
+def run_thermal(args):
+    """THERMAL 256x256x400 (oven surrounded, seeded oven temperature): one step = one full
+    Solver::run with -DTHERMAL semantics (Jacobi to the reference's stop rule, five outer
+    iterations). Reports grid-pt*z-steps/s of the z-marches, Jacobi voxel-sweeps/s and the
+    heat-sweep kernel's roofline from live CUDA events."""
+    import torch
+    from shg_focused_gaussian_beams_gb300.solver import Solver, heat_sweeps
+    inst = W.config_thermal_256()
+    s = Solver(crystal=W.CRYSTAL_QPM50, nx=inst.nx, ny=inst.ny, nz=inst.nz, lx=inst.lx, ly=inst.ly, thermal=True,
+               bc=inst.bc)
+    times = []
+    with Clocks(0) as clk:
+        for k in range(args.warmup + args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            s.run(inst.power, inst.waist, inst.focal, inst.temp, inst.t_inf, inst.t1, inst.t2)
+            torch.cuda.synchronize()
+            if k >= args.warmup:
+                times.append(time.perf_counter() - t0)
+    counts = s.jacobi_counts()
+    outer = sum(1 for c in counts if c >= 0)
+    sweeps = sum(c for c in counts if c >= 0)
+    t = statistics.median(times)
+    vox = inst.nx * inst.ny * inst.nz
+    # heat-sweep kernel alone: CUDA events around 200 sweeps on the same grid
+    T = np.full((inst.nz, inst.ny, inst.nx), inst.temp, np.float32)
+    Q = np.zeros_like(T)
+    from shg_focused_gaussian_beams_gb300 import _lib
+    import ctypes as C
+    cfg = _lib.default_config(nx=inst.nx, ny=inst.ny, nz=inst.nz, lx=inst.lx, ly=inst.ly)
+    t0 = time.perf_counter()
+    heat_sweeps(W.CRYSTAL_QPM50, T, Q, 25.0, 2, inst.bc, lx=inst.lx, ly=inst.ly)
+    t_small = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    heat_sweeps(W.CRYSTAL_QPM50, T, Q, 25.0, 402, inst.bc, lx=inst.lx, ly=inst.ly)
+    per_sweep = (time.perf_counter() - t0 - t_small) / 400
+    peak, peak_kind = measured_hbm()
+    ach = 12.0 * vox / per_sweep / 1e9
+    line = {"metric": "THERMAL 256x256x400 solve: grid-pt·z-steps/s of the z-marches", "impl": "ours",
+            "value": vox * outer / t, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * t, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "thermal256: 256x256x400, P=30 W, xi=2.84, 2000x1000 um cross-section, "
+                                   "oven-surrounded faces at a seeded U(45,55) C", "t_oven": inst.temp},
+            "jacobi_counts": counts, "voxel_sweeps_per_s": vox * sweeps / t,
+            "roofline": {"bound": "hbm", "kernel": "k_heat<1>", "achieved": ach, "peak": peak, "unit": "GB/s",
+                         "frac": ach / peak, "peak_source": peak_kind, "ms_per_launch": 1e3 * per_sweep,
+                         "algorithmic_bytes_per_launch": 12.0 * vox, "traffic": None,
+                         "note": "per-sweep time from 400 back-to-back sweeps on the host clock"},
+            "clocks": clk.summary(), "efficiency": s.efficiency()}
+    print(json.dumps(line), flush=True)
+
+
 def cpu_sample(insts, cores):
     """Bounded CPU sample: one solve per core from the workload, N <= 128 and Nz <= 200
     (the CPU's per-point cost grows with N, so this flatters the CPU)."""
@@ -308,9 +361,11 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["sweep", "plain128", "rows256"], default="sweep")
+    ap.add_argument("--workload", choices=["sweep", "plain128", "rows256", "thermal256"], default="sweep")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.workload == "thermal256":
+        run_thermal(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
