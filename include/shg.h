@@ -82,6 +82,19 @@ int shg_efficiency(shg_handle *h, double *eta);
 
 const char *shg_last_error(void);
 
+/* ---- Gradients (adjoint z-march, no counterpart in the reference) ---------------- */
+/* Gradient of the output SH power L = 1/2 eps0 c n_s dx dy sum|S_out|^2 of the plain CWES
+ * (shg_cwes_device semantics, fields at the top of slice NZ-1) with respect to the input
+ * fields (grad_pump / grad_sh: device, NX*NY complex64, as dL/dRe + i dL/dIm; either may be
+ * NULL), the oven temperature (input fields held fixed) and the poling period.
+ * `checkpoints` states are kept in the forward pass (segments replayed backwards).
+ * out4: [0] L (W), [1] dL/dT (W/K), [2] dL/dLambda (W/um), [3] dL/d(delta k) (W um).
+ * Synchronises `stream`. */
+int shg_grad_device(shg_handle *h, float temp, const void *pump_in, const void *sh_in, int checkpoints,
+                    void *grad_pump, void *grad_sh, double *out4, void *stream);
+/* Changes the poling period (Crystal.h:43) of a plain handle for the following runs. */
+int shg_set_poling_period(shg_handle *h, float lambda_qpm);
+
 /* ---- THERMAL (cfg.thermal = 1) ----------------------------------------------------- */
 /* After shg_run on a thermal handle: the final temperature tensor (NX*NY*NZ floats,
  * Tfield::Tfinal) and the Jacobi sweep count of each of the five outer iterations of

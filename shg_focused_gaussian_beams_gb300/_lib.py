@@ -66,6 +66,8 @@ SIGNATURES = {
     "shg_batch_launch_count": (_i, [_vp, _pi]),
     "shg_batch_io_bytes": (_i, [_vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "shg_dft2d_device": (_i, [_i, _i, _vp, _vp, _vp]),
+    "shg_grad_device": (_i, [_vp, _f, _vp, _vp, _i, _vp, _vp, _pd, _vp]),
+    "shg_set_poling_period": (_i, [_vp, _f]),
     "shg_get_temperature": (_i, [_vp, _pf]),
     "shg_get_jacobi_counts": (_i, [_vp, _pi]),
     "shg_init_temperature": (_i, [C.POINTER(Config), _f, _f, _f, _i, _pf]),

@@ -1,0 +1,38 @@
+// Adjoint z-march: device launchers and the host driver.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "shg_internal.h"
+#include "shg_march.cuh"
+
+namespace shg {
+
+cudaError_t launch_rk4_state(float2 *P, float2 *S, int nn, const float4 *stepc, int s, const InstDesc *d,
+                             cudaStream_t st);
+cudaError_t launch_rk4_vjp(const float2 *P0, const float2 *S0, float2 *cP, float2 *cS, int nn, const float4 *stepc,
+                           int s, const InstDesc *d, double *acc_step, cudaStream_t st);
+cudaError_t launch_colpass(int n, int mode, float2 *A, const float2 *H, float2 *F, const InstDesc *d, double *acc,
+                           cudaStream_t st);
+cudaError_t launch_abs2_sum(const float2 *S, int nn, double *out, cudaStream_t st);
+cudaError_t launch_seed_cotangent(const float2 *S, float2 *cP, float2 *cS, int nn, float g, cudaStream_t st);
+
+// Device work space of one gradient pass.
+struct AdjointWork {
+    ~AdjointWork();
+    int ensure(int n, int K, int L, int nck);
+    void release();
+    int n = 0, K = 0, L = 0, nck = 0;
+    void *mem = nullptr;
+    size_t bytes = 0;
+    float2 *X = nullptr, *cot = nullptr, *ck = nullptr, *Xs = nullptr, *Ws = nullptr, *Fs = nullptr;
+    double *acc_step = nullptr, *acc_glob = nullptr;
+};
+
+// One gradient pass of the solve described by (h host copy, d device copy) whose P / S
+// hold the input fields and whose propagators / step constants are set up. out[0] = loss
+// (SH output power, W), out[1] = dL/dT, out[2] = dL/dLambda, out[3] = dL/d(delta k).
+int adjoint_run(const shg_config &cfg, const InstDesc &h, const InstDesc *d, float temp, int checkpoints,
+                AdjointWork &w, cudaStream_t st, float2 *grad_pump, float2 *grad_sh, double *out);
+
+}  // namespace shg

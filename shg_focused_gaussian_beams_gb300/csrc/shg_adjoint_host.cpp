@@ -1,0 +1,213 @@
+// Gradient of the output SH power of a plain solve (adjoint z-march with checkpoints).
+//
+// Forward: the solve is marched once, saving the state every L steps (L = ceil(K/C) for
+// C checkpoints, K = NZ-1 steps). Backward: segment by segment from the last, the segment
+// is replayed from its checkpoint (keeping the step-start state X_s, the diffraction
+// output W_s and the spectrum F_s), then the cotangent is carried back through
+// RK4^T(W_s), the adjoint diffraction, and RK4^T(X_s). Parameter gradients come from
+// per-step FP64 sums: the coupling constants i*kappa*exp(-+i z dk) carry dk (hence the
+// poling period and T), kappa_p,s = pi dQ / (n lambda) and the TPA factor carry n(T), the
+// propagators carry k = 2 pi n / lambda. The oven temperature enters through n_p(T) and
+// n_s(T) (Sellmeier, Crystal.h:116-132, differentiated analytically); the input fields are
+// held fixed.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/shg.h"
+#include "shg_adjoint.h"
+#include "shg_internal.h"
+
+namespace shg {
+
+#define AD_CUDA(call)                                                                                  \
+    do {                                                                                               \
+        cudaError_t e_ = (call);                                                                       \
+        if (e_ != cudaSuccess) {                                                                       \
+            set_error(std::string("adjoint: ") + #call + ": " + cudaGetErrorString(e_));              \
+            return e_ == cudaErrorMemoryAllocation ? SHG_ERR_NOMEM : SHG_ERR_CUDA;                     \
+        }                                                                                              \
+    } while (0)
+
+AdjointWork::~AdjointWork() { release(); }
+
+void AdjointWork::release() {
+    if (mem) cudaFree(mem);
+    mem = nullptr;
+    bytes = 0;
+}
+
+int AdjointWork::ensure(int n_, int K_, int L_, int nck_) {
+    if (mem && n == n_ && K == K_ && L == L_ && nck == nck_) return SHG_OK;
+    release();
+    n = n_;
+    K = K_;
+    L = L_;
+    nck = nck_;
+    const size_t nn = (size_t)n * n;
+    const size_t st = 2 * nn;  // one state: P then S
+    // X (2 fields), cot (2), checkpoints (nck states), segment X_s, W_s, F_s (L states each),
+    // per-step sums (K x 8 doubles), propagator sums + loss (8 doubles)
+    bytes = sizeof(float2) * (st * (2 + (size_t)nck + 3 * (size_t)L)) + sizeof(double) * (8 * (size_t)K + 8);
+    AD_CUDA(cudaMalloc(&mem, bytes));
+    float2 *p = reinterpret_cast<float2 *>(mem);
+    X = p;
+    p += st;
+    cot = p;
+    p += st;
+    ck = p;
+    p += st * nck;
+    Xs = p;
+    p += st * L;
+    Ws = p;
+    p += st * L;
+    Fs = p;
+    p += st * L;
+    acc_step = reinterpret_cast<double *>(p);
+    acc_glob = acc_step + 8 * (size_t)K;
+    return SHG_OK;
+}
+
+// dn/dT of Crystal.h:116-132 in double (the smooth model behind the float index).
+static double sellmeier_dT(double L, double T) {
+    const double A = 4.502483, B = 0.007294, C = 0.185087, D = -0.02357, E = 0.073423, F = 0.199595, G = 0.001,
+                 H = 7.99724;
+    const double tk = T + 273.15;
+    const double b = 3.483933e-8 * tk * tk, c = 1.607839e-8 * tk * tk;
+    const double db = 2 * 3.483933e-8 * tk, dc = 2 * 1.607839e-8 * tk;
+    const double L2 = L * L;
+    const double den = L2 - (C + c) * (C + c);
+    const double n2 = A + (B + b) / den + E / (L2 - F * F) + G / (L2 - H * H) + D * L2;
+    const double dn2 = db / den + (B + b) * 2 * (C + c) * dc / (den * den);
+    return dn2 / (2 * std::sqrt(n2));
+}
+
+static int rows2(int n, int sign, float2 *A, cudaStream_t st) {
+    const size_t nn = (size_t)n * n;
+    AD_CUDA(launch_dft_rows(n, sign, A, A, st));
+    AD_CUDA(launch_dft_rows(n, sign, A + nn, A + nn, st));
+    return SHG_OK;
+}
+
+// X <- D(X) (both fields); spectra stored in F (2 fields) when F != nullptr.
+static int diffraction_fwd(int n, float2 *X, float2 *F, const InstDesc &h, const InstDesc *d, cudaStream_t st) {
+    const size_t nn = (size_t)n * n;
+    int rc = rows2(n, +1, X, st);
+    if (rc) return rc;
+    AD_CUDA(launch_colpass(n, 0, X, h.Hp, F, d, nullptr, st));
+    AD_CUDA(launch_colpass(n, 0, X + nn, h.Hs, F ? F + nn : nullptr, d, nullptr, st));
+    return rows2(n, -1, X, st);
+}
+
+// c <- D^H(c) with the propagator sensitivities added to acc[0], acc[1].
+static int diffraction_adj(int n, float2 *c, float2 *F, const InstDesc &h, const InstDesc *d, double *acc,
+                           cudaStream_t st) {
+    const size_t nn = (size_t)n * n;
+    int rc = rows2(n, +1, c, st);
+    if (rc) return rc;
+    AD_CUDA(launch_colpass(n, 1, c, h.Hp, F, d, acc + 0, st));
+    AD_CUDA(launch_colpass(n, 1, c + nn, h.Hs, F + nn, d, acc + 1, st));
+    return rows2(n, -1, c, st);
+}
+
+static int rk4_state(int n, float2 *X, const InstDesc &h, const InstDesc *d, int s, cudaStream_t st) {
+    const int nn = n * n;
+    AD_CUDA(launch_rk4_state(X, X + nn, nn, h.stepc, s, d, st));
+    return SHG_OK;
+}
+
+int adjoint_run(const shg_config &cfg, const InstDesc &h, const InstDesc *d, float temp, int checkpoints,
+                AdjointWork &w, cudaStream_t st, float2 *grad_pump, float2 *grad_sh, double *out) {
+    const int n = h.n, K = h.nsteps;
+    const size_t nn = (size_t)n * n, sb = 2 * nn * sizeof(float2);
+    if (checkpoints < 1) checkpoints = 1;
+    if (checkpoints > K) checkpoints = K;
+    const int L = (K + checkpoints - 1) / checkpoints;
+    const int nseg = (K + L - 1) / L;
+    int rc = w.ensure(n, K, L, nseg);
+    if (rc) return rc;
+    AD_CUDA(cudaMemsetAsync(w.acc_step, 0, sizeof(double) * (8 * (size_t)K + 8), st));
+    // P and S of the solve hold the input fields after the set-up.
+    AD_CUDA(cudaMemcpyAsync(w.X, h.P, nn * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+    AD_CUDA(cudaMemcpyAsync(w.X + nn, h.S, nn * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+    // forward with checkpoints
+    for (int s = 0; s < K; ++s) {
+        if (s % L == 0) AD_CUDA(cudaMemcpyAsync(w.ck + (size_t)(s / L) * 2 * nn, w.X, sb, cudaMemcpyDeviceToDevice, st));
+        if ((rc = rk4_state(n, w.X, h, d, s, st))) return rc;
+        if ((rc = diffraction_fwd(n, w.X, nullptr, h, d, st))) return rc;
+        if ((rc = rk4_state(n, w.X, h, d, s, st))) return rc;
+    }
+    // loss: P_SH = 1/2 eps0 c n_s dx dy sum |S_out|^2
+    double *lsum = w.acc_glob + 2;
+    AD_CUDA(launch_abs2_sum(w.X + nn, (int)nn, lsum, st));
+    const float lp = cfg.lp, ls = (float)(0.5 * (double)lp);
+    const float ns = sellmeier(ls, temp), np = sellmeier(lp, temp);
+    const double kl = field_power(1.0, ns, h.dx, h.dy);
+    AD_CUDA(launch_seed_cotangent(w.X + nn, w.cot, w.cot + nn, (int)nn, (float)(2.0 * kl), st));
+    // backward
+    for (int seg = nseg - 1; seg >= 0; --seg) {
+        const int s0 = seg * L, s1 = std::min(K, s0 + L);
+        AD_CUDA(cudaMemcpyAsync(w.X, w.ck + (size_t)seg * 2 * nn, sb, cudaMemcpyDeviceToDevice, st));
+        for (int s = s0; s < s1; ++s) {
+            const size_t j = (size_t)(s - s0) * 2 * nn;
+            AD_CUDA(cudaMemcpyAsync(w.Xs + j, w.X, sb, cudaMemcpyDeviceToDevice, st));
+            if ((rc = rk4_state(n, w.X, h, d, s, st))) return rc;
+            if ((rc = diffraction_fwd(n, w.X, w.Fs + j, h, d, st))) return rc;
+            AD_CUDA(cudaMemcpyAsync(w.Ws + j, w.X, sb, cudaMemcpyDeviceToDevice, st));
+            if ((rc = rk4_state(n, w.X, h, d, s, st))) return rc;
+        }
+        for (int s = s1 - 1; s >= s0; --s) {
+            const size_t j = (size_t)(s - s0) * 2 * nn;
+            double *as = w.acc_step + 8 * (size_t)s;
+            AD_CUDA(launch_rk4_vjp(w.Ws + j, w.Ws + j + nn, w.cot, w.cot + nn, (int)nn, h.stepc, s, d, as, st));
+            if ((rc = diffraction_adj(n, w.cot, w.Fs + j, h, d, w.acc_glob, st))) return rc;
+            AD_CUDA(launch_rk4_vjp(w.Xs + j, w.Xs + j + nn, w.cot, w.cot + nn, (int)nn, h.stepc, s, d, as, st));
+        }
+    }
+    if (grad_pump) AD_CUDA(cudaMemcpyAsync(grad_pump, w.cot, nn * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+    if (grad_sh) AD_CUDA(cudaMemcpyAsync(grad_sh, w.cot + nn, nn * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+    // parameter gradients on the host
+    std::vector<double> acc(8 * (size_t)K + 8);
+    std::vector<float4> stepc(K);
+    AD_CUDA(cudaMemcpyAsync(acc.data(), w.acc_step, acc.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    AD_CUDA(cudaMemcpyAsync(stepc.data(), h.stepc, K * sizeof(float4), cudaMemcpyDeviceToHost, st));
+    AD_CUDA(cudaStreamSynchronize(st));
+    const double *g = acc.data() + 8 * (size_t)K;
+    const double loss = kl * g[2];
+    double dL_ddk = 0, dL_dkp = 0, dL_dks = 0, dL_dtpa = 0;
+    float z = 0.0f;
+    for (int s = 0; s < K; ++s) {
+        const double *a = acc.data() + 8 * (size_t)s;
+        const double aPr = stepc[s].x, aPi = stepc[s].y, aSr = stepc[s].z, aSi = stepc[s].w;
+        // d alpha_P / d theta = -i alpha_P, d alpha_S / d theta = i alpha_S
+        const double dth = (a[0] * aPi + a[1] * (-aPr)) + (a[2] * (-aSi) + a[3] * aSr);
+        dL_ddk += (double)z * dth;
+        dL_dkp += a[0] * aPr + a[1] * aPi;
+        dL_dks += a[2] * aSr + a[3] * aSi;
+        dL_dtpa += a[4];
+        z += h.dz;
+    }
+    dL_dkp /= (double)h.kp;
+    dL_dks /= (double)h.ks;
+    const double kpw = 2.0 * 3.14159265358979323846 * (double)np / (double)lp;
+    const double ksw = 2.0 * 3.14159265358979323846 * (double)ns / (double)ls;
+    const double dL_dkpw = g[0] * (double)h.dz * (double)h.gp / kpw;
+    const double dL_dksw = g[1] * (double)h.dz * (double)h.gs / ksw;
+    const double dnp = sellmeier_dT(lp, temp), dns = sellmeier_dT(ls, temp);
+    const double two_pi = 2.0 * 3.14159265358979323846;
+    const double ddk_dT = two_pi * (2.0 * dnp / lp - dns / ls);
+    const double dT = dL_ddk * ddk_dT + dL_dkp * (-(double)h.kp / np) * dnp + dL_dks * (-(double)h.ks / ns) * dns +
+                      dL_dtpa * ((double)h.tpa1 / ns) * dns + dL_dkpw * (two_pi / lp) * dnp +
+                      dL_dksw * (two_pi / ls) * dns + loss / ns * dns;
+    const double lam = (double)cfg.lambda_qpm;
+    out[0] = loss;
+    out[1] = dT;
+    out[2] = dL_ddk * (-two_pi / (lam * lam));
+    out[3] = dL_ddk;
+    return SHG_OK;
+}
+
+}  // namespace shg

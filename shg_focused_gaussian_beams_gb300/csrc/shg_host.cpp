@@ -18,6 +18,7 @@
 #include "shg_internal.h"
 #include "shg_march.cuh"
 #include "shg_thermal_host.h"
+#include "shg_adjoint.h"
 
 #include <memory>
 
@@ -142,7 +143,8 @@ int ensure_twiddles(int device) {
             const double a = 2.0 * 3.14159265358979323846264338327950288 * (double)m / (double)N;
             tab[N + m] = make_float2((float)std::cos(a), (float)(-std::sin(a)));
         }
-    for (const float2 *addr : {twiddle_symbol_address_march(), twiddle_symbol_address_thermal()}) {
+    for (const float2 *addr :
+         {twiddle_symbol_address_march(), twiddle_symbol_address_thermal(), twiddle_symbol_address_adjoint()}) {
         void *p = const_cast<float2 *>(addr);
         if (!p) {
             set_error("twiddle table symbol unavailable");
@@ -252,6 +254,25 @@ class Batch {
         SHG_CUDA(cudaMemset(pool_, 0, pool_bytes_));
         desc_dirty_ = true;
         return SHG_OK;
+    }
+
+    // Replace the crystal constants (grid fields ignored) and refresh every descriptor.
+    void set_crystal(const shg_config &c) {
+        const int nx = cr_.nx, ny = cr_.ny, nz = cr_.nz, dev = cr_.device;
+        const float lx = cr_.lx, ly = cr_.ly;
+        cr_ = c;
+        cr_.nx = nx;
+        cr_.ny = ny;
+        cr_.nz = nz;
+        cr_.lx = lx;
+        cr_.ly = ly;
+        cr_.device = dev;
+        for (int i = 0; i < (int)desc_.size(); ++i) {
+            const int keep_given = desc_[i].pump_given;
+            fill_scalars(cr_, sp_[i], desc_[i]);
+            desc_[i].pump_given = keep_given;
+        }
+        desc_dirty_ = true;
     }
 
     // Re-parameterise solve i (same grid) without reallocating.
@@ -400,7 +421,34 @@ class Batch {
         return SHG_OK;
     }
 
+    // Upload descriptors, place the input fields and run only the set-up kernels
+    // (propagators, step constants, input power): the state the adjoint starts from.
+    int setup_only(cudaStream_t st) {
+        if (desc_dirty_) {
+            SHG_CUDA(cudaMemcpyAsync(d_desc_, desc_.data(), desc_.size() * sizeof(InstDesc), cudaMemcpyHostToDevice, st));
+            desc_dirty_ = false;
+        }
+        SHG_TRY_INT(enqueue_inputs(st));
+        SHG_CUDA(launch_setup(d_desc_, (int)desc_.size(), max_nn_, max_nz_, st));
+        return SHG_OK;
+    }
+
+    const InstDesc *device_desc() const { return d_desc_; }
+
    private:
+    int enqueue_inputs(cudaStream_t st) {
+        SHG_CUDA(cudaMemsetAsync(acc_, 0, 4 * sizeof(double) * desc_.size(), st));
+        for (int i = 0; i < (int)desc_.size(); ++i) {
+            const size_t bytes = (size_t)desc_[i].n * desc_[i].n * sizeof(float2);
+            if (p_src_[i]) SHG_CUDA(cudaMemcpyAsync(desc_[i].P, p_src_[i], bytes, cudaMemcpyDeviceToDevice, st));
+            if (s_src_[i])
+                SHG_CUDA(cudaMemcpyAsync(desc_[i].S, s_src_[i], bytes, cudaMemcpyDeviceToDevice, st));
+            else
+                SHG_CUDA(cudaMemsetAsync(desc_[i].S, 0, bytes, st));
+        }
+        return SHG_OK;
+    }
+
     int enqueue(cudaStream_t st, Recorder *rec = nullptr) {
         SHG_CUDA(cudaMemsetAsync(acc_, 0, 4 * sizeof(double) * desc_.size(), st));
         for (int i = 0; i < (int)desc_.size(); ++i) {
@@ -511,6 +559,7 @@ struct shg_handle {
     shg_config cfg;
     Batch batch;
     std::unique_ptr<ThermalSolve> th;  // set for thermal configurations
+    std::unique_ptr<AdjointWork> adj;  // work space of gradient passes
     SolveParams sp{};
     int n = 0;
     float2 *stage_p = nullptr, *stage_s = nullptr;  // device staging of given input fields
@@ -806,6 +855,49 @@ int shg_efficiency(shg_handle *h, double *eta) {
         set_error("efficiency is not finite");
         return SHG_ERR_NONFINITE;
     }
+    return SHG_OK;
+}
+
+int shg_grad_device(shg_handle *h, float temp, const void *pump_in, const void *sh_in, int checkpoints,
+                    void *grad_pump, void *grad_sh, double *out4, void *stream) {
+    SHG_TRY(check_handle(h));
+    if (h->th) {
+        set_error("shg_grad_device: gradients are for plain handles (hold the temperature field fixed)");
+        return SHG_ERR_STATE;
+    }
+    if (!pump_in || !out4) {
+        set_error("shg_grad_device: pump_in and out4 are required");
+        return SHG_ERR_INVALID;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t bytes = (size_t)h->n * h->n * sizeof(float2);
+    SHG_CUDA(cudaMemcpyAsync(h->stage_p, pump_in, bytes, cudaMemcpyDeviceToDevice, st));
+    if (sh_in) SHG_CUDA(cudaMemcpyAsync(h->stage_s, sh_in, bytes, cudaMemcpyDeviceToDevice, st));
+    h->pump_given = true;
+    h->sh_given = sh_in != nullptr;
+    h->have_pump = true;
+    h->sp.temp = temp;
+    h->sp.tprop = temp;
+    SHG_TRY(h->batch.set_params(0, h->sp));
+    h->batch.set_sources(0, h->stage_p, h->sh_given ? h->stage_s : nullptr);
+    SHG_TRY(h->batch.setup_only(st));
+    if (!h->adj) h->adj.reset(new AdjointWork);
+    return adjoint_run(h->cfg, h->batch.desc(0), h->batch.device_desc(), temp, checkpoints, *h->adj, st,
+                       static_cast<float2 *>(grad_pump), static_cast<float2 *>(grad_sh), out4);
+}
+
+int shg_set_poling_period(shg_handle *h, float lambda_qpm) {
+    SHG_TRY(check_handle(h));
+    if (!(lambda_qpm != 0.0f) || !std::isfinite(lambda_qpm)) {
+        set_error("poling period must be finite and non-zero");
+        return SHG_ERR_INVALID;
+    }
+    h->cfg.lambda_qpm = lambda_qpm;
+    if (h->th) {
+        set_error("shg_set_poling_period: not for thermal handles");
+        return SHG_ERR_STATE;
+    }
+    h->batch.set_crystal(h->cfg);
     return SHG_OK;
 }
 

@@ -14,6 +14,7 @@ struct InstDesc;
 // Device addresses of every translation unit's twiddle-table copy (current device).
 const float2 *twiddle_symbol_address_march();
 const float2 *twiddle_symbol_address_thermal();
+const float2 *twiddle_symbol_address_adjoint();
 
 // shg_march.cu
 cudaError_t launch_setup(const InstDesc *inst, int n_inst, int max_nn, int max_nz, cudaStream_t st);
@@ -21,6 +22,7 @@ cudaError_t launch_rows(int n, const InstDesc *inst, const int *list, int count,
 cudaError_t launch_cols(int n, const InstDesc *inst, const int *list, int count, cudaStream_t st);
 bool line_length_supported(int n);
 cudaError_t launch_dft2d(int n, int sign, const float2 *in, float2 *out, cudaStream_t st);
+cudaError_t launch_dft_rows(int n, int sign, const float2 *in, float2 *out, cudaStream_t st);
 
 // shg_thermal.cu
 struct HeatCoef;

@@ -103,6 +103,23 @@ class Solver:
                                     sh_out.data_ptr(), st), "shg_cwes_device")
         return pump_out, sh_out
 
+    def set_poling_period(self, lambda_qpm):
+        check(lib().shg_set_poling_period(self._h, float(lambda_qpm)), "shg_set_poling_period")
+        self.cfg.lambda_qpm = float(lambda_qpm)
+
+    def grad(self, temp, pump_in, sh_in=None, checkpoints=20, stream=None):
+        """Adjoint pass: L = SH output power and its gradients with respect to the input
+        fields (torch complex64 CUDA tensors, dL/dRe + i dL/dIm), the oven temperature
+        (fields held fixed) and the poling period. Returns a dict."""
+        import torch
+        gp = torch.empty_like(pump_in)
+        gs = torch.empty_like(pump_in)
+        out = (C.c_double * 4)()
+        st = torch.cuda.current_stream(pump_in.device).cuda_stream if stream is None else stream
+        check(lib().shg_grad_device(self._h, temp, pump_in.data_ptr(), None if sh_in is None else sh_in.data_ptr(),
+                                    int(checkpoints), gp.data_ptr(), gs.data_ptr(), out, st), "shg_grad_device")
+        return {"loss": out[0], "grad_pump": gp, "grad_sh": gs, "dT": out[1], "dLambda": out[2], "ddk": out[3]}
+
     def fields(self):
         p = np.zeros((self.ny, self.nx), np.complex64)
         s = np.zeros((self.ny, self.nx), np.complex64)

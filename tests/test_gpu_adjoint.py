@@ -1,0 +1,126 @@
+"""Adjoint z-march against FP64 central finite differences (GB300 only).
+
+The finite differences use the oracle's FP64 run of the same method. The device march
+uses the reference's float delta-k; the FP64 model is pinned to that value at the base
+point and varies with T and the poling period as the double-precision model does
+(delta-k(T) = dk32(T0) + dk64(T) - dk64(T0)), so both differentiate the same function.
+Bar: agreement to 1e-3 (relative).
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():  # pragma: no cover - CPU containers
+    pytest.skip("no CUDA device", allow_module_level=True)
+
+from shg_focused_gaussian_beams_gb300 import workloads as W  # noqa: E402
+from shg_focused_gaussian_beams_gb300.autograd import gaussian_pump, shg_power  # noqa: E402
+from shg_focused_gaussian_beams_gb300.solver import Solver  # noqa: E402
+
+FD_RTOL = 1e-3
+N, NZ, T0, P0 = 64, 40, 50.0, 20.0
+
+
+def smooth_noise(rng, n, cells=8):
+    """Seeded complex Gaussian field smoothed over `cells` grid cells (FFT low-pass)."""
+    a = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    k = np.fft.fftfreq(n)
+    g = np.exp(-0.5 * (k[:, None] ** 2 + k[None, :] ** 2) * (2 * math.pi * cells / 2.355) ** 2)
+    b = np.fft.ifft2(np.fft.fft2(a) * g)
+    return b / np.sqrt(np.mean(np.abs(b) ** 2))
+
+
+@pytest.fixture(scope="module")
+def case():
+    inst = W.plain_instance(N, NZ, P0, 2.84, T0)
+    cfg = O.make_cfg(W.CRYSTAL_QPM50, N, N, NZ, inst.lx, inst.ly)
+    o = O.Oracle(cfg)
+    rng = np.random.default_rng(31)
+    pert = 1 + 0.05 * smooth_noise(rng, N)
+    pump64 = o.set_pump64(inst.power, inst.focal, inst.waist, T0) * pert
+    dk32 = float(o.dk_constant(T0))
+    s = Solver(crystal=W.CRYSTAL_QPM50, nx=N, ny=N, nz=NZ, lx=inst.lx, ly=inst.ly)
+    pump_t = torch.from_numpy(pump64.astype(np.complex64)).cuda()
+    r = s.grad(T0, pump_t, checkpoints=7)
+    torch.cuda.synchronize()
+    return dict(inst=inst, cfg=cfg, o=o, pump64=pump64, dk32=dk32, s=s, r=r, pert=pert, rng=rng)
+
+
+def loss64(c, pump64, T=T0, lam=None):
+    cfg = c["cfg"]
+    o = c["o"]
+    dk = c["dk32"] + (o.dk_constant64(T) - o.dk_constant64(T0))
+    if lam is not None:
+        dk += 2 * math.pi * (1.0 / lam - 1.0 / cfg.lambda_qpm)
+    _, so, _, _ = o.cwes_plain64(pump64, np.zeros_like(pump64), T, dk)
+    eps0 = float(np.float32(8.8541878128e-12 * 1e12 / 1e6))
+    cl = float(np.float32(299792458 * 1e6 / 1e12))
+    dx = float(np.float32(cfg.lx / (N - 1)))
+    dy = float(np.float32(cfg.ly / (N - 1)))
+    return 0.5 * eps0 * cl * o.n64(0.532, T) * dx * dy * float(np.sum(np.abs(so) ** 2))
+
+
+def test_loss_matches_fp64(case):
+    L = loss64(case, case["pump64"])
+    assert abs(case["r"]["loss"] - L) / L < 1e-4
+
+
+def test_field_gradient_vs_fd(case):
+    g = case["r"]["grad_pump"].cpu().numpy().astype(np.complex128)
+    p = case["pump64"]
+    rng = np.random.default_rng(7)
+    adj, fd = [], []
+    for _ in range(8):
+        d = smooth_noise(rng, N) * p  # directions shaped like the beam
+        eps = 1e-4 * np.linalg.norm(p) / np.linalg.norm(d)
+        fd.append((loss64(case, p + eps * d) - loss64(case, p - eps * d)) / (2 * eps))
+        adj.append(float(np.sum(np.real(np.conj(g) * d))))
+    adj, fd = np.array(adj), np.array(fd)
+    assert np.linalg.norm(adj - fd) / np.linalg.norm(fd) < FD_RTOL, (adj, fd)
+
+
+def test_temperature_gradient_vs_fd(case):
+    h = 1e-4 * T0
+    fd = (loss64(case, case["pump64"], T=T0 + h) - loss64(case, case["pump64"], T=T0 - h)) / (2 * h)
+    assert abs(case["r"]["dT"] - fd) / abs(fd) < FD_RTOL, (case["r"]["dT"], fd)
+
+
+def test_poling_period_gradient_vs_fd(case):
+    """delta-k moves by 2 pi h / Lambda^2 per step h: over the 30 mm crystal a relative step
+    of 1e-4 turns the phase by 2.4 rad, far outside the linear range, so the step is 1e-7."""
+    lam = case["cfg"].lambda_qpm
+    h = 1e-7 * lam
+    fd = (loss64(case, case["pump64"], lam=lam + h) - loss64(case, case["pump64"], lam=lam - h)) / (2 * h)
+    assert abs(case["r"]["dLambda"] - fd) / abs(fd) < FD_RTOL, (case["r"]["dLambda"], fd)
+
+
+def test_checkpoint_count_does_not_change_the_gradient(case):
+    r2 = case["s"].grad(T0, torch.from_numpy(case["pump64"].astype(np.complex64)).cuda(), checkpoints=NZ - 1)
+    g1 = case["r"]["grad_pump"].cpu().numpy()
+    g2 = r2["grad_pump"].cpu().numpy()
+    assert np.linalg.norm(g1 - g2) / np.linalg.norm(g1) < 1e-5
+    assert abs(r2["dT"] - case["r"]["dT"]) / abs(case["r"]["dT"]) < 1e-5
+
+
+def test_autograd_focus_and_temperature(case):
+    """torch.autograd through the adjoint: focus gradient via a torch-built pump."""
+    inst = case["inst"]
+    pert = torch.from_numpy(case["pert"]).cuda()
+    focal = torch.tensor(inst.focal, dtype=torch.float64, device="cuda", requires_grad=True)
+    temp = torch.tensor(T0, dtype=torch.float64, device="cuda", requires_grad=True)
+    pump = gaussian_pump(N, N, inst.lx, inst.ly, inst.power, inst.waist, focal, T0) * pert
+    L = shg_power(case["s"], pump, temp, case["cfg"].lambda_qpm, checkpoints=7)
+    L.backward()
+    o = case["o"]
+    h = 1e-4 * inst.focal
+    Lp = loss64(case, o.set_pump64(inst.power, inst.focal + h, inst.waist, T0) * case["pert"])
+    Lm = loss64(case, o.set_pump64(inst.power, inst.focal - h, inst.waist, T0) * case["pert"])
+    fd = (Lp - Lm) / (2 * h)
+    assert abs(focal.grad.item() - fd) / abs(fd) < FD_RTOL, (focal.grad.item(), fd)
+    assert abs(temp.grad.item() - case["r"]["dT"]) / abs(case["r"]["dT"]) < 1e-6
