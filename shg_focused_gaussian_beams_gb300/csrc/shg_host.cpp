@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -143,8 +144,8 @@ int ensure_twiddles(int device) {
             const double a = 2.0 * 3.14159265358979323846264338327950288 * (double)m / (double)N;
             tab[N + m] = make_float2((float)std::cos(a), (float)(-std::sin(a)));
         }
-    for (const float2 *addr :
-         {twiddle_symbol_address_march(), twiddle_symbol_address_thermal(), twiddle_symbol_address_adjoint()}) {
+    for (const float2 *addr : {twiddle_symbol_address_march(), twiddle_symbol_address_thermal(),
+                               twiddle_symbol_address_adjoint(), twiddle_symbol_address_resident()}) {
         void *p = const_cast<float2 *>(addr);
         if (!p) {
             set_error("twiddle table symbol unavailable");
@@ -249,6 +250,22 @@ class Batch {
             }
             classes_.push_back(c);
         }
+        resident_ = !(std::getenv("SHG_MARCH") && std::string(std::getenv("SHG_MARCH")) == "streaming");
+        for (auto &c : classes_) {
+            for (int k = 0; k < c.count; ++k) c.pt_steps += (double)c.n * c.n * c.steps[k];
+            if (resident_) SHG_CUDA(prepare_resident(c.n, &c.max_clusters));
+        }
+        // resident march: class streams (largest solves first) and one job counter per class
+        while ((int)side_streams_.size() < (int)classes_.size()) {
+            cudaStream_t s2;
+            SHG_CUDA(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+            side_streams_.push_back(s2);
+            cudaEvent_t e2;
+            SHG_CUDA(cudaEventCreateWithFlags(&e2, cudaEventDisableTiming));
+            side_events_.push_back(e2);
+        }
+        if (!fork_event_) SHG_CUDA(cudaEventCreateWithFlags(&fork_event_, cudaEventDisableTiming));
+        SHG_CUDA(cudaMalloc(&d_counters_, 64 * sizeof(int)));
         SHG_CUDA(cudaMalloc(&d_lists_, lists.size() * sizeof(int)));
         SHG_CUDA(cudaMemcpy(d_lists_, lists.data(), lists.size() * sizeof(int), cudaMemcpyHostToDevice));
         SHG_CUDA(cudaMemset(pool_, 0, pool_bytes_));
@@ -336,6 +353,7 @@ class Batch {
 
     int launch_count() const {
         int c = 2;  // set-up kernels
+        if (resident_) return c + (int)classes_.size();
         for (const auto &k : classes_) {
             const int K = k.steps.empty() ? 0 : k.steps[0];
             c += (K + 1) + K;
@@ -380,6 +398,8 @@ class Batch {
     struct Class {
         int n = 0, offset = 0, count = 0;
         std::vector<int> steps;  // descending
+        int max_clusters = 0;    // resident march: clusters resident at once
+        double pt_steps = 0;     // sum of n*n*nsteps
     };
 
    public:
@@ -462,6 +482,32 @@ class Batch {
         if (rec) SHG_TRY_INT(rec->begin("setup", 24.0 * (double)total_points(), st));
         SHG_CUDA(launch_setup(d_desc_, (int)desc_.size(), max_nn_, max_nz_, st));
         if (rec) SHG_TRY_INT(rec->end(st));
+        if (resident_) {
+            SHG_CUDA(cudaMemsetAsync(d_counters_, 0, 64 * sizeof(int), st));
+            // classes in descending grid size; concurrently on side streams unless timed
+            std::vector<int> order(classes_.size());
+            for (int i = 0; i < (int)order.size(); ++i) order[i] = i;
+            std::sort(order.begin(), order.end(), [&](int a, int b) { return classes_[a].n > classes_[b].n; });
+            if (!rec) SHG_CUDA(cudaEventRecord(fork_event_, st));
+            for (int oi = 0; oi < (int)order.size(); ++oi) {
+                const Class &k = classes_[order[oi]];
+                const int *list = d_lists_ + k.offset;
+                int *counter = d_counters_ + order[oi];
+                if (rec) {
+                    SHG_TRY_INT(rec->begin("resident<" + std::to_string(k.n) + ">", 32.0 * k.pt_steps, st));
+                    SHG_CUDA(launch_resident(k.n, d_desc_, list, k.count, counter, k.max_clusters, st));
+                    SHG_TRY_INT(rec->end(st));
+                } else {
+                    cudaStream_t ss = side_streams_[oi];
+                    SHG_CUDA(cudaStreamWaitEvent(ss, fork_event_, 0));
+                    SHG_CUDA(launch_resident(k.n, d_desc_, list, k.count, counter, k.max_clusters, ss));
+                    SHG_CUDA(cudaEventRecord(side_events_[oi], ss));
+                }
+            }
+            if (!rec)
+                for (int oi = 0; oi < (int)order.size(); ++oi) SHG_CUDA(cudaStreamWaitEvent(st, side_events_[oi], 0));
+            return SHG_OK;
+        }
         for (const auto &k : classes_) {
             const int K = k.steps[0];
             const int *list = d_lists_ + k.offset;
@@ -507,6 +553,8 @@ class Batch {
 
     void release() {
         invalidate_graph();
+        if (d_counters_) cudaFree(d_counters_);
+        d_counters_ = nullptr;
         if (capture_stream_) cudaStreamDestroy(capture_stream_);
         capture_stream_ = nullptr;
         if (pool_) cudaFree(pool_);
@@ -533,6 +581,11 @@ class Batch {
     bool desc_dirty_ = true;
     cudaGraphExec_t graph_exec_ = nullptr;
     cudaStream_t capture_stream_ = nullptr;
+    bool resident_ = true;
+    int *d_counters_ = nullptr;
+    std::vector<cudaStream_t> side_streams_;
+    std::vector<cudaEvent_t> side_events_;
+    cudaEvent_t fork_event_ = nullptr;
 };
 
 int validate_config(const shg_config &c) {

@@ -136,3 +136,21 @@ def test_errors_are_reported():
         s.fields()
     with pytest.raises(ShgError, match="STATE"):
         s.cwes(50.0)
+
+
+def test_resident_march_equals_streaming_march(monkeypatch):
+    """The resident (shared-memory) march runs the same arithmetic as the streaming
+    row/column kernels: identical output fields for every size class."""
+    insts = W.config_sweep(count=512, seed=77)
+    pick = [i for i in insts if i.nx == 64][:5] + [i for i in insts if i.nx == 128][:4] + \
+        [i for i in insts if i.nx == 256][:3]
+    pick = [W.Instance(**{**i.as_dict(), "nz": min(i.nz, 60)}) for i in pick]
+    a = Sweep(pick, crystal=W.CRYSTAL_QPM50)
+    eta_a, fa = a.run(with_fields=True)
+    monkeypatch.setenv("SHG_MARCH", "streaming")
+    b = Sweep(pick, crystal=W.CRYSTAL_QPM50)
+    eta_b, fb = b.run(with_fields=True)
+    assert a.launch_count() < b.launch_count()
+    for x, y in zip(fa, fb):
+        assert np.array_equal(x, y)
+    np.testing.assert_allclose(eta_a, eta_b, rtol=1e-12, atol=0)
