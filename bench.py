@@ -66,6 +66,42 @@ def workload(name, rank=0):
     return insts, desc
 
 
+def heat_sweep_time(inst, nsweeps):
+    """Mean time of one heat sweep (CUDA events on the launching stream) on device buffers."""
+    import ctypes as C
+    import torch
+    from shg_focused_gaussian_beams_gb300 import _lib
+    from shg_focused_gaussian_beams_gb300.solver import _cfg_from, init_temperature
+    cfg = _cfg_from(W.CRYSTAL_QPM50, nx=inst.nx, ny=inst.ny, nz=inst.nz, lx=inst.lx, ly=inst.ly)
+    T0 = init_temperature(W.CRYSTAL_QPM50, inst.nx, inst.ny, inst.nz, inst.temp, inst.temp, inst.temp, inst.bc,
+                          lx=inst.lx, ly=inst.ly)
+    Ta = torch.from_numpy(T0).cuda()
+    Tb = Ta.clone()
+    QK = torch.full_like(Ta, 1e-4)
+    st = torch.cuda.current_stream()
+    L = _lib.lib()
+    _lib.check(L.shg_heat_sweeps_device(C.byref(cfg), Ta.data_ptr(), Tb.data_ptr(), QK.data_ptr(), 25.0, 4, inst.bc,
+                                        st.cuda_stream), "shg_heat_sweeps_device")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    _lib.check(L.shg_heat_sweeps_device(C.byref(cfg), Ta.data_ptr(), Tb.data_ptr(), QK.data_ptr(), 25.0, nsweeps,
+                                        inst.bc, st.cuda_stream), "shg_heat_sweeps_device")
+    e1.record(st)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) * 1e-3 / nsweeps
+
+
+def run_heat(args):
+    """Heat sweeps alone on the 256x256x400 THERMAL grid (profiling case)."""
+    inst = W.config_thermal_256()
+    per = heat_sweep_time(inst, max(args.steps, 1) * 100)
+    vox = inst.nx * inst.ny * inst.nz
+    peak, kind = measured_hbm()
+    print(json.dumps({"workload": "heat256", "ms_per_sweep": 1e3 * per, "GBps_algorithmic": 12.0 * vox / per / 1e9,
+                      "frac": 12.0 * vox / per / 1e9 / peak, "peak_source": kind}), flush=True)
+
+
 def run_thermal(args):
     """THERMAL 256x256x400 (oven surrounded, seeded oven temperature): one step = one full
     Solver::run with -DTHERMAL semantics (Jacobi to the reference's stop rule, five outer
@@ -90,18 +126,7 @@ def run_thermal(args):
     sweeps = sum(c for c in counts if c >= 0)
     t = statistics.median(times)
     vox = inst.nx * inst.ny * inst.nz
-    # heat-sweep kernel alone: CUDA events around 200 sweeps on the same grid
-    T = np.full((inst.nz, inst.ny, inst.nx), inst.temp, np.float32)
-    Q = np.zeros_like(T)
-    from shg_focused_gaussian_beams_gb300 import _lib
-    import ctypes as C
-    cfg = _lib.default_config(nx=inst.nx, ny=inst.ny, nz=inst.nz, lx=inst.lx, ly=inst.ly)
-    t0 = time.perf_counter()
-    heat_sweeps(W.CRYSTAL_QPM50, T, Q, 25.0, 2, inst.bc, lx=inst.lx, ly=inst.ly)
-    t_small = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    heat_sweeps(W.CRYSTAL_QPM50, T, Q, 25.0, 402, inst.bc, lx=inst.lx, ly=inst.ly)
-    per_sweep = (time.perf_counter() - t0 - t_small) / 400
+    per_sweep = heat_sweep_time(inst, 400)
     peak, peak_kind = measured_hbm()
     ach = 12.0 * vox / per_sweep / 1e9
     line = {"metric": "THERMAL 256x256x400 solve: grid-pt·z-steps/s of the z-marches", "impl": "ours",
@@ -114,7 +139,7 @@ def run_thermal(args):
             "roofline": {"bound": "hbm", "kernel": "k_heat<1>", "achieved": ach, "peak": peak, "unit": "GB/s",
                          "frac": ach / peak, "peak_source": peak_kind, "ms_per_launch": 1e3 * per_sweep,
                          "algorithmic_bytes_per_launch": 12.0 * vox, "traffic": None,
-                         "note": "per-sweep time from 400 back-to-back sweeps on the host clock"},
+                         "note": "CUDA events around 400 back-to-back sweeps on the launching stream"},
             "clocks": clk.summary(), "efficiency": s.efficiency()}
     print(json.dumps(line), flush=True)
 
@@ -361,10 +386,12 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["sweep", "plain128", "rows256", "thermal256"], default="sweep")
+    ap.add_argument("--workload", choices=["sweep", "plain128", "rows256", "thermal256", "heat256"], default="sweep")
     args = ap.parse_args()
     if args.workload == "thermal256":
         run_thermal(args)
+    elif args.workload == "heat256":
+        run_heat(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -108,6 +108,11 @@ int shg_get_jacobi_counts(shg_handle *h, int *counts5);
 int shg_init_temperature(const shg_config *cfg, float temp, float t1, float t2, int bc, float *T_out);
 int shg_heat_sweeps(const shg_config *cfg, float *T_inout, const float *Q, float t_inf, int nsweeps, int bc);
 int shg_dk_thermal(const shg_config *cfg, const float *T, float *DK, float *NP, float *NS);
+/* `nsweeps` heat sweeps on device buffers: Ta holds T on entry, Tb an identical copy (the
+ * voxels the stencil never writes must match); sweep k writes the other buffer, so the
+ * result is in Ta for even nsweeps and in Tb for odd. QK = Q / k_th per voxel. */
+int shg_heat_sweeps_device(const shg_config *cfg, void *Ta, void *Tb, const void *QK, float t_inf, int nsweeps, int bc,
+                           void *stream);
 
 /* ---- Batched sweep: many independent plain solves in one device schedule ----------- */
 typedef struct shg_instance {

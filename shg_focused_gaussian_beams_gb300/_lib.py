@@ -73,6 +73,7 @@ SIGNATURES = {
     "shg_init_temperature": (_i, [C.POINTER(Config), _f, _f, _f, _i, _pf]),
     "shg_heat_sweeps": (_i, [C.POINTER(Config), _pf, _pf, _f, _i, _i]),
     "shg_dk_thermal": (_i, [C.POINTER(Config), _pf, _pf, _pf, _pf]),
+    "shg_heat_sweeps_device": (_i, [C.POINTER(Config), _vp, _vp, _vp, _f, _i, _i, _vp]),
     "shg_cwes_noalloc": (_i, [C.POINTER(Config), _f, _vp, _vp, _vp, _vp, _pd, _vp]),
 }
 

@@ -38,6 +38,8 @@ cudaError_t launch_init_temperature(float *T, int nx, int ny, int nz, float temp
                                     cudaStream_t st);
 cudaError_t launch_heat(float *Tf, const float *Ti, const float *QK, const HeatCoef &c, int nx, int ny, int nz,
                         int bc, cudaStream_t st);
+cudaError_t verify_fast_division(float d, float r, unsigned long long *d_count, unsigned long long *mismatches,
+                                 cudaStream_t st);
 cudaError_t launch_sq_diff_sum(const float *Tf, const float *Ti, size_t n, double *out, cudaStream_t st);
 cudaError_t launch_sellmeier_tables(const float *T, float *NP, float *NS, float *DK, size_t n, float lp, float ls,
                                     float two_pi, float inv_lambda, cudaStream_t st);

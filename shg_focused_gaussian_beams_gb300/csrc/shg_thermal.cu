@@ -9,6 +9,9 @@
 // so delta-k(T) is bit-identical too.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+#include <string>
+
 #include "shg_internal.h"
 #include "shg_thermal.cuh"
 
@@ -93,6 +96,179 @@ __global__ void __launch_bounds__(256) k_heat(float *__restrict__ Tf, const floa
         s = __fadd_rn(s, __fmul_rn(c.CV, t[zn]));
         s = __fadd_rn(s, c.tinfBiD);
         Tf[i] = __fmul_rn(s, c.GV);
+    }
+}
+
+// a / d for the interior stencil: the corrected product where it was verified equal to the
+// IEEE quotient, IEEE division otherwise.
+__device__ __forceinline__ float div_const(float a, float d, float r, int fast) {
+    const unsigned e = (__float_as_uint(a) >> 23) & 0xffu;
+    if (fast && e - kDivExpLo <= kDivExpHi - kDivExpLo) {
+        const float q = a * r;
+        const float rem = fmaf(-q, d, a);
+        return fmaf(rem, r, q);
+    }
+    return __fdiv_rn(a, d);
+}
+
+// Exhaustive check of the corrected product against IEEE division for every float of
+// either sign with biased exponent in [kDivExpLo, kDivExpHi]: counts mismatches.
+__global__ void k_verify_div(float d, float r, unsigned long long *mismatch) {
+    const unsigned long long span = (unsigned long long)(kDivExpHi - kDivExpLo + 1) << 23;
+    unsigned long long bad = 0;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < 2 * span;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const unsigned sign = i >= span ? 0x80000000u : 0u;
+        const unsigned bits = sign | (unsigned)(((unsigned long long)kDivExpLo << 23) + (i % span));
+        const float a = __uint_as_float(bits);
+        const float q1 = __fdiv_rn(a, d);
+        const float q = a * r;
+        const float rem = fmaf(-q, d, a);
+        const float q2 = fmaf(rem, r, q);
+        bad += __float_as_uint(q1) != __float_as_uint(q2);
+    }
+    for (int o = 16; o > 0; o >>= 1) bad += __shfl_xor_sync(0xffffffffu, bad, o);
+    if ((threadIdx.x & 31) == 0 && bad) atomicAdd(mismatch, bad);
+}
+
+cudaError_t verify_fast_division(float d, float r, unsigned long long *d_count, unsigned long long *mismatches,
+                                 cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+    k_verify_div<<<1216, 256, 0, st>>>(d, r, d_count);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpyAsync(mismatches, d_count, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(st);
+}
+
+// One voxel of Tfield.h:113-258 from its six face neighbours (only those the formula of
+// the voxel's class uses are read): xm/xp, ym/yp, zm/zp = T at x-1/x+1, y-1/y+1, z-1/z+1.
+// Returns false for voxels the reference never writes.
+template <int BC>
+__device__ __forceinline__ bool heat_voxel(const HeatCoef &c, int x, int y, int z, int nx, int ny, int nz, float xm,
+                                           float xp, float ym, float yp, float zm, float zp, float qk, float &out) {
+    const bool xi = x > 0 && x < nx - 1, yi = y > 0 && y < ny - 1, zi = z > 0 && z < nz - 1;
+    if (xi && yi && zi) {
+        const float a = div_const(__fadd_rn(xp, xm), c.dx2, c.rdx2, c.fast_div);
+        const float b = div_const(__fadd_rn(yp, ym), c.dy2, c.rdy2, c.fast_div);
+        const float d = div_const(__fadd_rn(zp, zm), c.dz2, c.rdz2, c.fast_div);
+        out = __fmul_rn(c.L2, __fadd_rn(__fadd_rn(__fadd_rn(a, b), d), qk));
+        return true;
+    }
+    const float tzn = z == 0 ? zp : zm;
+    if (xi && yi) {  // back / front faces
+        float s = __fadd_rn(tzn, __fmul_rn(c.az, __fadd_rn(xp, xm)));
+        s = __fadd_rn(s, __fmul_rn(c.bz, __fadd_rn(yp, ym)));
+        s = __fadd_rn(s, c.tinfBiz);
+        out = __fdiv_rn(s, c.den_z);
+        return true;
+    }
+    if (BC != 0) return false;
+    const bool xe = x == 0 || x == nx - 1, ze = z == 0 || z == nz - 1, ytop = y == ny - 1;
+    const float txn = x == 0 ? xp : xm;
+    if (xe && yi && zi) {
+        float s = __fadd_rn(txn, __fmul_rn(c.ax, __fadd_rn(yp, ym)));
+        s = __fadd_rn(s, __fmul_rn(c.bx, __fadd_rn(zp, zm)));
+        s = __fadd_rn(s, c.tinfBix);
+        out = __fdiv_rn(s, c.den_x);
+    } else if (xi && ytop && zi) {
+        float s = __fadd_rn(ym, __fmul_rn(c.ay, __fadd_rn(xp, xm)));
+        s = __fadd_rn(s, __fmul_rn(c.by, __fadd_rn(zp, zm)));
+        s = __fadd_rn(s, c.tinfBiy);
+        out = __fdiv_rn(s, c.den_y);
+    } else if (xe && yi && ze) {
+        const float s = __fadd_rn(__fadd_rn(__fmul_rn(c.av, txn), __fmul_rn(c.bv, tzn)), __fmul_rn(c.cv, __fadd_rn(yp, ym)));
+        out = __double2float_rn(__dmul_rn(__dadd_rn((double)s, c.KV), (double)c.V));
+    } else if (ytop && xi && ze) {
+        const float s = __fadd_rn(__fadd_rn(__fmul_rn(c.ah, ym), __fmul_rn(c.bh, tzn)), __fmul_rn(c.ch, __fadd_rn(xm, xp)));
+        out = __double2float_rn(__dmul_rn(__dadd_rn((double)s, c.KH), (double)c.H));
+    } else if (xe && ytop && zi) {
+        const float s = __fadd_rn(__fadd_rn(__fmul_rn(c.ad, ym), __fmul_rn(c.bd, txn)), __fmul_rn(c.cd, __fadd_rn(zp, zm)));
+        out = __double2float_rn(__dmul_rn(__dadd_rn((double)s, c.KD), (double)c.D));
+    } else if (xe && ytop && ze) {
+        float s = __fadd_rn(__fmul_rn(c.AV, txn), __fmul_rn(c.BV, ym));
+        s = __fadd_rn(s, __fmul_rn(c.CV, tzn));
+        s = __fadd_rn(s, c.tinfBiD);
+        out = __fmul_rn(s, c.GV);
+    } else {
+        return false;
+    }
+    return true;
+}
+
+// 2.5D form of the same sweep: a 32x8 (x, y) tile marches a z range; each thread keeps
+// T(z-1), T(z), T(z+1) of its column in registers and reads its x / y neighbours from a
+// shared-memory copy of the current plane with a one-voxel halo. Every global load (the
+// column's T, Q/k and the halo values) is issued two planes before it is used, so the
+// DRAM latency overlaps the work of the planes in between instead of sitting between the
+// two barriers of one plane.
+constexpr int HT_X = 32, HT_Y = 8, HT_Z = 25;
+template <int BC>
+__global__ void __launch_bounds__(HT_X * HT_Y) k_heat25(float *__restrict__ Tf, const float *__restrict__ Ti,
+                                                        const float *__restrict__ QK, const HeatCoef c, int nx, int ny,
+                                                        int nz) {
+    __shared__ float pl[HT_Y + 2][HT_X + 2];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int x = blockIdx.x * HT_X + tx, y = blockIdx.y * HT_Y + ty;
+    const int z0 = blockIdx.z * HT_Z, z1 = min(nz, z0 + HT_Z);
+    const bool in = x < nx && y < ny;
+    const size_t sxy = (size_t)nx * ny;
+    const size_t col = (size_t)y * nx + x;
+    // halo roles: a neighbour row (y-1 or y+1) and a neighbour column (x-1 or x+1)
+    int hx = -1, hy = -1, sx = 0, sy = 0;
+    if (ty == 0 && y > 0) { hx = x; hy = y - 1; sx = tx + 1; sy = 0; }
+    if (ty == HT_Y - 1 && y + 1 < ny) { hx = x; hy = y + 1; sx = tx + 1; sy = HT_Y + 1; }
+    int hx2 = -1, hy2 = -1, sx2 = 0, sy2 = 0;
+    if (tx == 0 && x > 0) { hx2 = x - 1; hy2 = y; sx2 = 0; sy2 = ty + 1; }
+    if (tx == HT_X - 1 && x + 1 < nx) { hx2 = x + 1; hy2 = y; sx2 = HT_X + 1; sy2 = ty + 1; }
+    const bool h1 = in && hx >= 0, h2 = in && hx2 >= 0;
+    const size_t hcol = h1 ? (size_t)hy * nx + hx : 0, hcol2 = h2 ? (size_t)hy2 * nx + hx2 : 0;
+    // column pointers advance by one plane per step
+    const float *pT = Ti + col, *pH = Ti + hcol, *pH2 = Ti + hcol2, *pQ = QK + col;
+    float *pO = Tf + col;
+    auto ldT = [&](int z) { return (in && z >= 0 && z < nz) ? pT[(size_t)z * sxy] : 0.f; };
+    float tm = ldT(z0 - 1), tc = ldT(z0), tp = ldT(z0 + 1), f1 = ldT(z0 + 2);
+    const float *qz = pQ + (size_t)z0 * sxy, *tz3 = pT + (size_t)(z0 + 3) * sxy;
+    const float *hz = pH + (size_t)z0 * sxy, *hz2 = pH2 + (size_t)z0 * sxy;
+    float *oz = pO + (size_t)z0 * sxy;
+    float q0 = (in && z0 < z1) ? qz[0] : 0.f, q1 = (in && z0 + 1 < z1) ? qz[sxy] : 0.f;
+    float a0 = (h1 && z0 < z1) ? hz[0] : 0.f, a1 = (h1 && z0 + 1 < z1) ? hz[sxy] : 0.f;
+    float b0 = (h2 && z0 < z1) ? hz2[0] : 0.f, b1 = (h2 && z0 + 1 < z1) ? hz2[sxy] : 0.f;
+    const size_t two = 2 * sxy;
+    for (int z = z0; z < z1; ++z) {
+        const float f2 = (in && z + 3 < nz) ? *tz3 : 0.f;
+        const bool nx2 = z + 2 < z1;
+        const float q2 = (in && nx2) ? qz[two] : 0.f;
+        const float a2 = (h1 && nx2) ? hz[two] : 0.f;
+        const float b2 = (h2 && nx2) ? hz2[two] : 0.f;
+        tz3 += sxy;
+        qz += sxy;
+        hz += sxy;
+        hz2 += sxy;
+        pl[ty + 1][tx + 1] = tc;
+        if (h1) pl[sy][sx] = a0;
+        if (h2) pl[sy2][sx2] = b0;
+        __syncthreads();
+        if (in) {
+            float out;
+            if (heat_voxel<BC>(c, x, y, z, nx, ny, nz, pl[ty + 1][tx], pl[ty + 1][tx + 2], pl[ty][tx + 1],
+                               pl[ty + 2][tx + 1], tm, tp, q0, out))
+                *oz = out;
+        }
+        oz += sxy;
+        __syncthreads();
+        tm = tc;
+        tc = tp;
+        tp = f1;
+        f1 = f2;
+        q0 = q1;
+        q1 = q2;
+        a0 = a1;
+        a1 = a2;
+        b0 = b1;
+        b1 = b2;
     }
 }
 
@@ -329,6 +505,16 @@ cudaError_t launch_init_temperature(float *T, int nx, int ny, int nz, float temp
 
 cudaError_t launch_heat(float *Tf, const float *Ti, const float *QK, const HeatCoef &c, int nx, int ny, int nz,
                         int bc, cudaStream_t st) {
+    static const bool simple = std::getenv("SHG_HEAT") && std::string(std::getenv("SHG_HEAT")) == "simple";
+    if (!simple) {
+        dim3 blk(HT_X, HT_Y, 1);
+        dim3 grd((nx + HT_X - 1) / HT_X, (ny + HT_Y - 1) / HT_Y, (nz + HT_Z - 1) / HT_Z);
+        if (bc == 0)
+            k_heat25<0><<<grd, blk, 0, st>>>(Tf, Ti, QK, c, nx, ny, nz);
+        else
+            k_heat25<1><<<grd, blk, 0, st>>>(Tf, Ti, QK, c, nx, ny, nz);
+        return cudaGetLastError();
+    }
     dim3 blk(32, 8, 1);
     dim3 grd((nx + 31) / 32, (ny + 7) / 8, nz);
     if (bc == 0)

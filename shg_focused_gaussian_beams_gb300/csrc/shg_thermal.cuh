@@ -17,7 +17,15 @@ struct HeatCoef {
     float tinf;
     double KV, KH, KD;           // 0.5*T_inf*(Bix+Biz), 0.5*T_inf*(Biy+Biz), 0.5*T_inf*(Bix+Biy)
     float tinfBix, tinfBiy, tinfBiz, tinfBiD;
+    // Division of the interior stencil by dx^2, dy^2, dz^2: when fast_div is set, a / d is
+    // formed as q = a*r, q + (a - q*d)*r with r = 1/d rounded, which was checked against
+    // IEEE division for every float a with biased exponent in [kDivExpLo, kDivExpHi]
+    // (verify_fast_division); other numerators use IEEE division.
+    float rdx2, rdy2, rdz2;
+    int fast_div;
 };
+
+constexpr unsigned kDivExpLo = 27, kDivExpHi = 227;  // |a| in [2^-100, 2^101)
 
 // Thermal extension of one solve.
 struct ThermDesc {

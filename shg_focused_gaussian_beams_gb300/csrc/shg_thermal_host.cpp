@@ -5,7 +5,11 @@
 
 #include <cmath>
 #include <cstring>
+#include <cstdlib>
+#include <map>
+#include <mutex>
 #include <random>
+#include <utility>
 #include <string>
 
 #include "../../include/shg.h"
@@ -78,6 +82,37 @@ HeatCoef make_heat_coef(const shg_config &cfg, float T_inf) {
     return c;
 }
 
+int enable_fast_division(HeatCoef &c, cudaStream_t st) {
+    static std::mutex mu;
+    static std::map<std::pair<int, unsigned>, bool> verified;  // (device, divisor bits) -> exact
+    static std::map<int, unsigned long long *> counters;
+    c.rdx2 = 1.0f / c.dx2;
+    c.rdy2 = 1.0f / c.dy2;
+    c.rdz2 = 1.0f / c.dz2;
+    c.fast_div = 0;
+    if (std::getenv("SHG_HEAT_DIV") && std::string(std::getenv("SHG_HEAT_DIV")) == "ieee") return SHG_OK;
+    int dev = 0;
+    TH_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    bool all = true;
+    for (float d : {c.dx2, c.dy2, c.dz2}) {
+        unsigned bits;
+        std::memcpy(&bits, &d, sizeof(bits));
+        auto key = std::make_pair(dev, bits);
+        auto it = verified.find(key);
+        if (it == verified.end()) {
+            unsigned long long *&cnt = counters[dev];
+            if (!cnt) TH_CUDA(cudaMalloc(&cnt, sizeof(unsigned long long)));
+            unsigned long long bad = 1;
+            TH_CUDA(verify_fast_division(d, 1.0f / d, cnt, &bad, st));
+            it = verified.emplace(key, bad == 0).first;
+        }
+        all = all && it->second;
+    }
+    c.fast_div = all ? 1 : 0;
+    return SHG_OK;
+}
+
 ThermalSolve::~ThermalSolve() {
     for (float *p : {T_[0], T_[1], qk_, np_, ns_, dk_, dkint_})
         if (p) cudaFree(p);
@@ -123,6 +158,7 @@ int ThermalSolve::sq_diff(float *out) {
 int ThermalSolve::sweeps(float t_inf, int n) {
     if (t_inf != tinf_coef_) {
         hc_ = make_heat_coef(cfg_, t_inf);
+        TH_TRY(enable_fast_division(hc_, st_));
         tinf_coef_ = t_inf;
     }
     for (int k = 0; k < n; ++k) {
@@ -326,6 +362,24 @@ int shg_heat_sweeps(const shg_config *cfg, float *T_inout, const float *Q, float
     TH_CUDA(cudaMemcpy(ts.T_prev(), T_inout, n * sizeof(float), cudaMemcpyHostToDevice));
     TH_TRY(ts.sweeps(t_inf, nsweeps));
     return ts.copy_temperature(T_inout);
+}
+
+int shg_heat_sweeps_device(const shg_config *cfg, void *Ta, void *Tb, const void *QK, float t_inf, int nsweeps, int bc,
+                           void *stream) {
+    TH_TRY(thermal_component_cfg(cfg));
+    if (!Ta || !Tb || !QK || nsweeps < 0) {
+        set_error("shg_heat_sweeps_device: bad argument");
+        return SHG_ERR_INVALID;
+    }
+    HeatCoef hc = make_heat_coef(*cfg, t_inf);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    TH_TRY(enable_fast_division(hc, st));
+    float *a = static_cast<float *>(Ta), *b = static_cast<float *>(Tb);
+    for (int k = 0; k < nsweeps; ++k) {
+        TH_CUDA(launch_heat(b, a, static_cast<const float *>(QK), hc, cfg->nx, cfg->ny, cfg->nz, bc, st));
+        std::swap(a, b);
+    }
+    return SHG_OK;
 }
 
 int shg_dk_thermal(const shg_config *cfg, const float *T, float *DK, float *NP, float *NS) {

@@ -12,6 +12,10 @@ namespace shg {
 
 // Tfield.h:118-125 coefficients with the reference's rounding.
 HeatCoef make_heat_coef(const shg_config &cfg, float t_inf);
+// Enables the corrected-product division of the interior stencil when it matches IEEE
+// division for every numerator in the checked exponent range, for all three divisors
+// (checked once per divisor value on the current device, results cached).
+int enable_fast_division(HeatCoef &c, cudaStream_t st);
 
 class ThermalSolve {
    public:
