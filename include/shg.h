@@ -56,10 +56,15 @@ int shg_destroy(shg_handle *h);
 /* Solver::run (Solver.h:279-355), same arguments in the same order. The output fields are
  * the state at the top of slice NZ-1 (what Solver::CWES saves as Pump_out/Signal_out,
  * Solver.h:250-255) and stay on the device until read. save_only_last / save_temperature
- * are accepted for signature parity; the Files.h text outputs are written by the `shg`
- * command line from the fields read back with shg_get_fields. */
+ * select the Files.h text outputs when an output directory is set (shg_set_output_dir). */
 int shg_run(shg_handle *h, float power, float waist, float focalpoint, float temp, float t_inf,
             float t_peltier1, float t_peltier2, int save_only_last, int save_temperature);
+/* Directory for the reference's text outputs (Files.h:19-79) written by shg_run: with
+ * save_only_last, Pump_out_{r,i}.dat / Signal_out_{r,i}.dat (top of slice NZ-1); without it,
+ * Pump_<s>_{r,i}.dat / Signal_<s>_{r,i}.dat for every slice s (Solver.h:250-262); with
+ * save_temperature on a thermal handle, Tfinal_<z>.dat (Solver.h:340). NULL or "" turns
+ * file output off (the default). */
+int shg_set_output_dir(shg_handle *h, const char *dir);
 
 /* Efields::setInputPump (Efields.h:174 -> setPump, Efields.h:74): Gaussian pump with the
  * refractive index taken at temperature tc. */
@@ -130,6 +135,9 @@ int shg_batch_destroy(shg_batch *b);
  * is not NULL it receives the SH output fields of all solves back to back in solve order
  * (solve i at the complex offset given by shg_batch_field_offsets). */
 int shg_batch_run(shg_batch *b, double *eta, float *sh_out_all);
+/* After a run: output pump and SH fields of all solves (same layout as sh_out_all above);
+ * either pointer may be NULL. */
+int shg_batch_fields(shg_batch *b, float *pump_out_all, float *sh_out_all);
 /* Replaces the run parameters of every solve (grids must stay the same); the next run
  * uploads them. */
 int shg_batch_set_instances(shg_batch *b, const shg_instance *inst, int n);

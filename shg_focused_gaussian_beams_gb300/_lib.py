@@ -58,6 +58,7 @@ SIGNATURES = {
     "shg_batch_create": (_i, [C.POINTER(Config), C.POINTER(Instance), _i, C.POINTER(_vp)]),
     "shg_batch_destroy": (_i, [_vp]),
     "shg_batch_run": (_i, [_vp, _pd, _vp]),
+    "shg_batch_fields": (_i, [_vp, _vp, _vp]),
     "shg_batch_set_instances": (_i, [_vp, C.POINTER(Instance), _i]),
     "shg_batch_field_offsets": (_i, [_vp, C.POINTER(C.c_longlong)]),
     "shg_batch_profile": (_i, [_vp, C.POINTER(KernelStat), _i, _pi]),
@@ -68,6 +69,7 @@ SIGNATURES = {
     "shg_dft2d_device": (_i, [_i, _i, _vp, _vp, _vp]),
     "shg_grad_device": (_i, [_vp, _f, _vp, _vp, _i, _vp, _vp, _pd, _vp]),
     "shg_set_poling_period": (_i, [_vp, _f]),
+    "shg_set_output_dir": (_i, [_vp, C.c_char_p]),
     "shg_get_temperature": (_i, [_vp, _pf]),
     "shg_get_jacobi_counts": (_i, [_vp, _pi]),
     "shg_init_temperature": (_i, [C.POINTER(Config), _f, _f, _f, _i, _pf]),

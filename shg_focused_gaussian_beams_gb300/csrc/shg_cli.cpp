@@ -21,18 +21,6 @@
 
 namespace {
 
-// Files.h:36-57: tab-separated, 20 significant digits, one row per y.
-void save_matrix_complex(const std::string &dir, const std::string &name, const std::vector<float> &v, int nx,
-                         int ny) {
-    for (int part = 0; part < 2; ++part) {
-        std::ofstream f(dir + "/" + name + (part == 0 ? "_r.dat" : "_i.dat"));
-        for (int iy = 0; iy < ny; ++iy) {
-            for (int ix = 0; ix < nx; ++ix) f << std::setprecision(20) << v[2 * ((size_t)iy * nx + ix) + part] << "\t";
-            f << "\n";
-        }
-    }
-}
-
 int fail(const char *what, int rc) {
     std::cerr << what << " failed (" << rc << "): " << shg_last_error() << std::endl;
     return 1;
@@ -103,13 +91,17 @@ int main(int argc, char **argv) {
     shg_handle *h = nullptr;
     int rc = shg_create(&cfg, &h);
     if (rc) return fail("shg_create", rc);
+    rc = shg_set_output_dir(h, outdir.c_str());
+    if (rc) return fail("shg_set_output_dir", rc);
+    // Solver.h:250-262 / 340: Pump_out/Signal_out (SOLS=1) or every slice (SOLS=0), Tfinal (STMP=1)
     rc = shg_run(h, Power, waist, focalpoint, Temp, T_inf, Tpeltier1, Tpeltier2, save_only_last, save_temperature);
     if (rc) return fail("shg_run", rc);
-    std::vector<float> pump((size_t)2 * cfg.nx * cfg.ny), sh(pump.size());
-    rc = shg_get_fields(h, pump.data(), sh.data());
-    if (rc) return fail("shg_get_fields", rc);
-    save_matrix_complex(outdir, "Pump_out", pump, cfg.nx, cfg.ny);
-    save_matrix_complex(outdir, "Signal_out", sh, cfg.nx, cfg.ny);
+    if (cfg.thermal) {
+        int counts[5];
+        if (shg_get_jacobi_counts(h, counts) == SHG_OK)
+            for (int i = 0; i < 5 && counts[i] >= 0; ++i)
+                std::cout << counts[i] << " iterations -> steady-state." << std::endl;
+    }
     double eta = 0;
     if (shg_efficiency(h, &eta) == SHG_OK) std::cout << "Conversion efficiency = " << std::setprecision(9) << eta << std::endl;
     shg_destroy(h);

@@ -306,6 +306,15 @@ class Batch {
         return SHG_OK;
     }
 
+    // Per-slice capture buffer of solve i (nullptr: off); slot 0 receives the input state.
+    void set_slices(int i, float2 *slices) {
+        if (desc_[i].slices != slices) {
+            desc_[i].slices = slices;
+            desc_dirty_ = true;
+            invalidate_graph();
+        }
+    }
+
     // Device buffers copied into P / S at the start of every run (nullptr: Gaussian pump
     // built on the device / SH cleared to zero).
     void set_sources(int i, const float2 *p_src, const float2 *s_src) {
@@ -389,6 +398,7 @@ class Batch {
     const InstDesc &desc(int i) const { return desc_[i]; }
     // SH output fields of all solves, contiguous in solve order; offset of solve i in points.
     const float2 *sout_all() const { return sout_all_; }
+    const float2 *pout_all() const { return desc_[0].Pout; }
     size_t field_offset(int i) const { return foff_[i]; }
     size_t total_points() const { return foff_.back(); }
     int size() const { return (int)desc_.size(); }
@@ -482,6 +492,13 @@ class Batch {
         if (rec) SHG_TRY_INT(rec->begin("setup", 24.0 * (double)total_points(), st));
         SHG_CUDA(launch_setup(d_desc_, (int)desc_.size(), max_nn_, max_nz_, st));
         if (rec) SHG_TRY_INT(rec->end(st));
+        for (int i = 0; i < (int)desc_.size(); ++i)
+            if (desc_[i].slices) {
+                const size_t nn = (size_t)desc_[i].n * desc_[i].n;
+                SHG_CUDA(cudaMemcpyAsync(desc_[i].slices, desc_[i].P, nn * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+                SHG_CUDA(cudaMemcpyAsync(desc_[i].slices + nn, desc_[i].S, nn * sizeof(float2),
+                                         cudaMemcpyDeviceToDevice, st));
+            }
         if (resident_) {
             SHG_CUDA(cudaMemsetAsync(d_counters_, 0, 64 * sizeof(int), st));
             // classes in descending grid size; concurrently on side streams unless timed
@@ -613,12 +630,15 @@ struct shg_handle {
     Batch batch;
     std::unique_ptr<ThermalSolve> th;  // set for thermal configurations
     std::unique_ptr<AdjointWork> adj;  // work space of gradient passes
+    std::string out_dir;               // Files.h outputs of shg_run when set
+    float2 *slices = nullptr;          // per-slice states for save_only_last = 0
     SolveParams sp{};
     int n = 0;
     float2 *stage_p = nullptr, *stage_s = nullptr;  // device staging of given input fields
     bool pump_given = false, sh_given = false, have_pump = false, have_result = false;
     cudaStream_t stream = nullptr;
     ~shg_handle() {
+        if (slices) cudaFree(slices);
         if (stage_p) cudaFree(stage_p);
         if (stage_s) cudaFree(stage_s);
         if (stream) cudaStreamDestroy(stream);
@@ -658,6 +678,42 @@ int handle_run(shg_handle *h, cudaStream_t st) {
     rc = b.run_async(st, true);
     if (rc) return rc;
     h->have_result = true;
+    return SHG_OK;
+}
+
+// Solver.h:250-262 and :340 outputs: Pump_out/Signal_out (top of slice NZ-1) or
+// Pump_<s>/Signal_<s> for every slice, and Tfinal_<z> when requested (THERMAL).
+int write_outputs(shg_handle *h, bool save_only_last, bool save_temperature) {
+    const int n = h->n, nz = h->cfg.nz;
+    const size_t nn = (size_t)n * n;
+    std::vector<float2> a(nn), b(nn);
+    if (save_only_last) {
+        SHG_TRY_INT(shg_get_fields(h, reinterpret_cast<float *>(a.data()), reinterpret_cast<float *>(b.data())));
+        if (!save_matrix_complex(h->out_dir, "Pump_out", a.data(), n, n) ||
+            !save_matrix_complex(h->out_dir, "Signal_out", b.data(), n, n)) {
+            set_error("cannot write output files in " + h->out_dir);
+            return SHG_ERR_INVALID;
+        }
+    } else {
+        std::vector<float2> all((size_t)nz * 2 * nn);
+        SHG_CUDA(cudaMemcpy(all.data(), h->slices, all.size() * sizeof(float2), cudaMemcpyDeviceToHost));
+        for (int s = 0; s < nz; ++s) {
+            const float2 *st = all.data() + (size_t)s * 2 * nn;
+            if (!save_matrix_complex(h->out_dir, "Pump_" + std::to_string(s), st, n, n) ||
+                !save_matrix_complex(h->out_dir, "Signal_" + std::to_string(s), st + nn, n, n)) {
+                set_error("cannot write output files in " + h->out_dir);
+                return SHG_ERR_INVALID;
+            }
+        }
+    }
+    if (save_temperature && h->th) {
+        std::vector<float> T(nn * (size_t)nz);
+        SHG_TRY_INT(h->th->copy_temperature(T.data()));
+        if (!save_tensor_real(h->out_dir, "Tfinal", T.data(), n, n, nz)) {
+            set_error("cannot write Tfinal files in " + h->out_dir);
+            return SHG_ERR_INVALID;
+        }
+    }
     return SHG_OK;
 }
 
@@ -845,8 +901,13 @@ int shg_run(shg_handle *h, float power, float waist, float focalpoint, float tem
     (void)save_only_last;
     (void)save_temperature;
     if (h->th) {
+        const bool per_slice = !h->out_dir.empty() && !save_only_last;
+        if (per_slice && !h->slices)
+            SHG_CUDA(cudaMalloc(&h->slices, (size_t)h->cfg.nz * 2 * h->n * h->n * sizeof(float2)));
+        h->th->set_slices(per_slice ? h->slices : nullptr);
         SHG_TRY(h->th->run(power, waist, focalpoint, temp, t_inf, t_peltier1, t_peltier2));
         h->have_result = true;
+        if (!h->out_dir.empty()) SHG_TRY(write_outputs(h, save_only_last, save_temperature));
         return SHG_OK;
     }
     // Solver.h:342-348: pump, SH start, propagators and delta-k all at Temp.
@@ -866,8 +927,13 @@ int shg_run(shg_handle *h, float power, float waist, float focalpoint, float tem
     } else {
         h->sh_given = false;
     }
+    const bool per_slice = !h->out_dir.empty() && !save_only_last;
+    if (per_slice && !h->slices)
+        SHG_CUDA(cudaMalloc(&h->slices, (size_t)h->cfg.nz * 2 * h->n * h->n * sizeof(float2)));
+    h->batch.set_slices(0, per_slice ? h->slices : nullptr);
     SHG_TRY(handle_run(h, h->stream));
     SHG_CUDA(cudaStreamSynchronize(h->stream));
+    if (!h->out_dir.empty()) SHG_TRY(write_outputs(h, save_only_last, false));
     return SHG_OK;
 }
 
@@ -937,6 +1003,12 @@ int shg_grad_device(shg_handle *h, float temp, const void *pump_in, const void *
     if (!h->adj) h->adj.reset(new AdjointWork);
     return adjoint_run(h->cfg, h->batch.desc(0), h->batch.device_desc(), temp, checkpoints, *h->adj, st,
                        static_cast<float2 *>(grad_pump), static_cast<float2 *>(grad_sh), out4);
+}
+
+int shg_set_output_dir(shg_handle *h, const char *dir) {
+    SHG_TRY(check_handle(h));
+    h->out_dir = dir ? dir : "";
+    return SHG_OK;
 }
 
 int shg_set_poling_period(shg_handle *h, float lambda_qpm) {
@@ -1046,6 +1118,18 @@ int shg_batch_run(shg_batch *b, double *eta, float *sh_out_all) {
                                  cudaMemcpyDeviceToHost, b->stream));
     SHG_CUDA(cudaStreamSynchronize(b->stream));
     if (eta) SHG_TRY(shg_batch_results(b, eta));
+    return SHG_OK;
+}
+
+int shg_batch_fields(shg_batch *b, float *pump_out_all, float *sh_out_all) {
+    if (!b || !b->ran) {
+        set_error("shg_batch_fields: batch has not run");
+        return SHG_ERR_STATE;
+    }
+    SHG_CUDA(cudaStreamSynchronize(b->stream));
+    const size_t bytes = b->batch.total_points() * sizeof(float2);
+    if (pump_out_all) SHG_CUDA(cudaMemcpy(pump_out_all, b->batch.pout_all(), bytes, cudaMemcpyDeviceToHost));
+    if (sh_out_all) SHG_CUDA(cudaMemcpy(sh_out_all, b->batch.sout_all(), bytes, cudaMemcpyDeviceToHost));
     return SHG_OK;
 }
 

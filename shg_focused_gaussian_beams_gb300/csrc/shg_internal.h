@@ -56,6 +56,10 @@ struct SolveParams {
     float tprop;  // index temperature of the propagators (beamPropagator, same centre value)
 };
 
+// shg_files.cpp (Files.h formats)
+bool save_matrix_complex(const std::string &dir, const std::string &name, const float2 *v, int nx, int ny);
+bool save_tensor_real(const std::string &dir, const std::string &name, const float *T, int nx, int ny, int nz);
+
 // shg_host.cpp
 void set_error(const std::string &msg);
 float sellmeier(float L, float T);

@@ -158,6 +158,15 @@ __global__ void __launch_bounds__(RowShape<N>::TPB) k_rows(const InstDesc *__res
     const float4 c1 = d.stepc[s - 1];
 #pragma unroll
     for (int r = 0; r < E; ++r) rk4_point(vp[r], vs[r], c1, d);
+    if (d.slices && s < d.nz) {
+        float2 *sl = d.slices + (size_t)s * 2 * N * N;
+#pragma unroll
+        for (int r = 0; r < E; ++r) {
+            const int k = spec_index<N, G>(t, r);
+            sl[base + k] = vp[r];
+            sl[(size_t)N * N + base + k] = vs[r];
+        }
+    }
     if (s == d.nsteps) {
         double aS = 0.0, aP = 0.0;
 #pragma unroll

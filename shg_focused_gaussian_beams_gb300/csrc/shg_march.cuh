@@ -16,6 +16,8 @@ struct InstDesc {
     float2 *Hp, *Hs;        // shifted propagators (Efields.h:107-126, 186-192) times 1/(n*n)
     float4 *stepc;          // per slice s: (kp*sin, kp*cos, -ks*sin, ks*cos) of z_s*dk
     double *acc;            // [0] sum |P_in|^2, [1] sum |S_out|^2, [2] sum |P_out|^2
+    float2 *slices;         // optional: state at the top of every slice s >= 1, P then S
+                            // (2*n*n per slice; the caller fills slice 0 with the input)
     int n;                  // NX = NY
     int nz;                 // slices
     int nsteps;             // SSFM steps run before the capture (nz - 1)

@@ -148,6 +148,15 @@ __global__ void __launch_bounds__(ResShape<N>::THREADS, 1)
                     const float4 c1 = d.stepc[s - 1];
 #pragma unroll
                     for (int r = 0; r < E; ++r) rk4_point(vp[r], vs[r], c1, d);
+                    if (d.slices && s < d.nz) {
+                        float2 *sl = d.slices + (size_t)s * 2 * N * N + (size_t)(rank * R + line) * N;
+#pragma unroll
+                        for (int r = 0; r < E; ++r) {
+                            const int k = spec_index<N, G>(t, r);
+                            sl[k] = vp[r];
+                            sl[(size_t)N * N + k] = vs[r];
+                        }
+                    }
                     if (s == K) {
                         const size_t base = (size_t)(rank * R + line) * N;
                         double aS = 0.0, aP = 0.0;

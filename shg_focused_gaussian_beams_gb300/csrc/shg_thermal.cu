@@ -458,6 +458,11 @@ __global__ void __launch_bounds__(ThRowShape<N>::TPB) k_rows_th(const InstDesc *
         const float Ip = th.qc * np1 * a2p, Is = th.qc * ns1 * a2s;
         const float Q = th.alpha_p * Ip + th.alpha_s * Is + th.beta_s * (Is * Is);
         th.QK[i3] = Q / th.kth;
+        if (d.slices && s < th.nz) {
+            float2 *sl = d.slices + (size_t)s * 2 * nxy;
+            sl[i2] = vp[r];
+            sl[nxy + i2] = vs[r];
+        }
         if (capture) {
             d.Pout[i2] = vp[r];
             d.Sout[i2] = vs[r];

@@ -248,7 +248,13 @@ int ThermalSolve::cwes(float power, float waist, float focal) {
     } else {
         TH_CUDA(cudaMemsetAsync(h_desc_.S, 0, nn * sizeof(float2), st_));
     }
+    h_desc_.slices = slices_;
+    TH_CUDA(cudaMemcpyAsync(d_desc_, &h_desc_, sizeof(InstDesc), cudaMemcpyHostToDevice, st_));
     TH_CUDA(launch_setup(d_desc_, 1, (int)nn, nz_, st_));
+    if (slices_) {
+        TH_CUDA(cudaMemcpyAsync(slices_, h_desc_.P, nn * sizeof(float2), cudaMemcpyDeviceToDevice, st_));
+        TH_CUDA(cudaMemcpyAsync(slices_ + nn, h_desc_.S, nn * sizeof(float2), cudaMemcpyDeviceToDevice, st_));
+    }
     const int *list0 = reinterpret_cast<const int *>(acc_ + 4);
     for (int s = 0; s <= nz_; ++s) {
         TH_CUDA(launch_rows_th(n_, d_desc_, th_, s, st_));

@@ -31,6 +31,8 @@ class ThermalSolve {
         for (int i = 0; i < 5; ++i) c[i] = counts_[i];
     }
     int powers(double *pin, double *psh, double *pout);
+    // Per-slice capture of every CWES (slot 0 = input state); nullptr: off.
+    void set_slices(float2 *s) { slices_ = s; }
     bool has_result() const { return have_result_; }
 
     // Components (device buffers owned here).
@@ -65,6 +67,7 @@ class ThermalSolve {
     float tc_ = 0.f, temp_ = 0.f;
     bool have_result_ = false;
     int sh_seed_ = -1;
+    float2 *slices_ = nullptr;
 };
 
 }  // namespace shg

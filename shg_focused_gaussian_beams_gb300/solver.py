@@ -76,6 +76,10 @@ class Solver:
                             int(save_temperature)), "shg_run")
         return self
 
+    def set_output_dir(self, path):
+        """Directory for the reference's text outputs of run() (Files.h formats)."""
+        check(lib().shg_set_output_dir(self._h, None if path is None else str(path).encode()), "shg_set_output_dir")
+
     # Efields::setInputPump (Efields.h:174)
     def set_input_pump(self, power, focalpoint, waist, tc):
         check(lib().shg_set_input_pump(self._h, power, focalpoint, waist, tc), "shg_set_input_pump")
@@ -196,6 +200,17 @@ class Sweep:
         off = self.field_offsets()
         fields = [np.asarray(buf)[off[i]:off[i + 1]].reshape(it.ny, it.nx) for i, it in enumerate(self.instances)]
         return eta, fields
+
+    def fields(self):
+        """Output (pump, SH) fields of every solve after a run: two lists of (n, n) arrays."""
+        off = self.field_offsets()
+        p = np.zeros(int(off[-1]), np.complex64)
+        s = np.zeros(int(off[-1]), np.complex64)
+        check(lib().shg_batch_fields(self._b, C.c_void_p(p.ctypes.data), C.c_void_p(s.ctypes.data)),
+              "shg_batch_fields")
+        sh = [(it.ny, it.nx) for it in self.instances]
+        return ([p[off[i]:off[i + 1]].reshape(sh[i]) for i in range(self.n)],
+                [s[off[i]:off[i + 1]].reshape(sh[i]) for i in range(self.n)])
 
     def set_instances(self, instances):
         arr = (_lib.Instance * self.n)()

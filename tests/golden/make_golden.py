@@ -70,6 +70,10 @@ def cli_case(tag, args, name):
         subprocess.run([exe] + [str(a) for a in args], cwd=d, check=True, stdout=subprocess.DEVNULL)
         po = _read_dat_complex(d, "Pump_out", r.ny, r.nx)
         so = _read_dat_complex(d, "Signal_out", r.ny, r.nx)
+        with open(os.path.join(d, "Signal_out_r.dat")) as fh:  # the reference's own text, first rows
+            head = [fh.readline() for _ in range(3)]
+        with open(os.path.join(HERE, "stock_cli_signal_head.txt"), "w") as fh:
+            fh.write("".join(head))
     np.savez_compressed(os.path.join(HERE, name), pump_out=po, sh_out=so, args=np.array(args, np.float64),
                         **crystal_meta(tag))
     print("wrote", name)
