@@ -47,9 +47,10 @@ def pt_steps(insts):
     return sum(i.nx * i.ny * i.nz for i in insts)
 
 
-def workload(name, rank=0):
+def workload(name, rank=0, world=1):
     if name == "sweep":
-        insts = W.config_sweep(count=512, seed=2024 + rank)
+        from shg_focused_gaussian_beams_gb300.parallel import rank_sweep
+        insts = rank_sweep(512, 2024, rank, world, "weak")
         desc = {"workload": "sweep512: 512 plain solves, N in {64,128,256}, Nz in {100,200,400}, P log-U(1,50) W, "
                             "xi U(0.5,5), T 50+-2 C, window 16 w0",
                 "solves": len(insts)}
@@ -253,13 +254,8 @@ def barrier(world):
 
 
 def allmax(world, v):
-    if world == 1:
-        return v
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    from shg_focused_gaussian_beams_gb300.parallel import world_max
+    return world_max(v) if world > 1 else v
 
 
 def run_reference(args):
@@ -300,7 +296,7 @@ def run_ours(args):
 
     world, rank, local = dist_setup(args.gpus)
     torch.cuda.set_device(local)
-    insts, desc = workload(args.workload, rank)
+    insts, desc = workload(args.workload, rank, world)
     sw = Sweep(insts, crystal=W.CRYSTAL_QPM50, device=local)
     stream = torch.cuda.Stream()
     for _ in range(max(args.warmup, 3)):
