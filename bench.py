@@ -93,6 +93,52 @@ def heat_sweep_time(inst, nsweeps):
     return e0.elapsed_time(e1) * 1e-3 / nsweeps
 
 
+def run_adjoint(args):
+    """Adjoint 256x256x400 (P = 20 W, xi = 2.84, Gaussian pump times a seeded 5 % smooth
+    perturbation, 20 checkpoints): time of the fused forward CWES and of the gradient pass
+    (forward with checkpoints + reverse sweep) through the C ABI, CUDA events."""
+    import torch
+    from shg_focused_gaussian_beams_gb300.autograd import gaussian_pump
+    from shg_focused_gaussian_beams_gb300.solver import Solver
+    inst = W.plain_instance(256, 400, 20.0, 2.84, 50.0)
+    g = torch.Generator().manual_seed(3)
+    noise = torch.randn(256, 256, 2, generator=g, dtype=torch.float64)
+    noise = torch.complex(noise[..., 0], noise[..., 1])
+    k = torch.fft.fftfreq(256, dtype=torch.float64)
+    lp = torch.exp(-0.5 * (k[:, None] ** 2 + k[None, :] ** 2) * (2 * 3.141592653589793 * 8 / 2.355) ** 2)
+    noise = torch.fft.ifft2(torch.fft.fft2(noise) * lp)
+    noise = noise / noise.abs().pow(2).mean().sqrt()
+    pump = (gaussian_pump(256, 256, inst.lx, inst.ly, inst.power, inst.waist, inst.focal, inst.temp, device="cpu")
+            * (1 + 0.05 * noise)).to(torch.complex64).cuda()
+    s = Solver(crystal=W.CRYSTAL_QPM50, nx=256, ny=256, nz=400, lx=inst.lx, ly=inst.ly)
+    st = torch.cuda.current_stream()
+    for _ in range(max(args.warmup, 1)):
+        s.cwes_device(inst.temp, pump)
+        s.grad(inst.temp, pump, checkpoints=20)
+    torch.cuda.synchronize()
+    def timed(fn, reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            fn()
+        e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+    fwd = timed(lambda: s.cwes_device(inst.temp, pump), max(args.steps, 1))
+    grd = timed(lambda: s.grad(inst.temp, pump, checkpoints=20), max(args.steps, 1))
+    r = s.grad(inst.temp, pump, checkpoints=20)
+    # every step stored (399 states of X_s, W_s, F_s: 1.2 GB), no replay
+    s.grad(inst.temp, pump, checkpoints=399)
+    torch.cuda.synchronize()
+    grd_all = timed(lambda: s.grad(inst.temp, pump, checkpoints=399), max(args.steps, 1))
+    r_all = s.grad(inst.temp, pump, checkpoints=399)
+    print(json.dumps({"workload": "adjoint256: 256x256x400, P=20 W, xi=2.84",
+                      "forward_ms": fwd, "gradient_ms_20_checkpoints": grd, "gradient_over_forward": grd / fwd,
+                      "gradient_ms_store_all": grd_all, "store_all_over_forward": grd_all / fwd,
+                      "loss_W": r["loss"], "dL_dT": r["dT"], "dL_dLambda": r["dLambda"],
+                      "store_all_dT_rel_diff": abs(r_all["dT"] - r["dT"]) / abs(r["dT"])}), flush=True)
+
+
 def run_heat(args):
     """Heat sweeps alone on the 256x256x400 THERMAL grid (profiling case)."""
     inst = W.config_thermal_256()
@@ -382,12 +428,14 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["sweep", "plain128", "rows256", "thermal256", "heat256"], default="sweep")
+    ap.add_argument("--workload", choices=["sweep", "plain128", "rows256", "thermal256", "heat256", "adjoint256"], default="sweep")
     args = ap.parse_args()
     if args.workload == "thermal256":
         run_thermal(args)
     elif args.workload == "heat256":
         run_heat(args)
+    elif args.workload == "adjoint256":
+        run_adjoint(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

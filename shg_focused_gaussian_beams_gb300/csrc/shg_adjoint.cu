@@ -147,13 +147,21 @@ __global__ void k_rk4_vjp(const float2 *__restrict__ P0, const float2 *__restric
 // where X is the transformed cotangent and q2 = dfX^2 tx^2 + dfY^2 ty^2 of the propagator
 // phase (Efields.h:121), so that acc * dz * g / k is the derivative of L w.r.t. the
 // wavenumber k = 2 pi n / lambda of that field.
+// Both fields in one launch: blockIdx.y = 0 pump (Hp), 1 SH (Hs); A and Fst hold the two
+// fields back to back, acc[field] receives the sums.
 template <int N, int MODE>
-__global__ void __launch_bounds__(16 * LineShape<N>::G) k_colpass(float2 *A, const float2 *__restrict__ H, float2 *Fst,
-                                                             const InstDesc *__restrict__ dd, double *acc) {
+__global__ void __launch_bounds__(16 * LineShape<N>::G) k_colpass(float2 *A0, float2 *Fst0,
+                                                             const InstDesc *__restrict__ dd, double *acc0) {
     constexpr int G = LineShape<N>::G, E = N / G, TC = 16;
     __shared__ float2 scratch[TC * E * G];
     const float2 *__restrict__ tab = g_twiddle + N;
     const InstDesc &d = *dd;
+    const int f = blockIdx.y;
+    const size_t nn = (size_t)N * N;
+    float2 *A = A0 + f * nn;
+    float2 *Fst = Fst0 ? Fst0 + f * nn : nullptr;
+    const float2 *__restrict__ H = f == 0 ? d.Hp : d.Hs;
+    double *acc = acc0 ? acc0 + f : nullptr;
     const int c = threadIdx.x % TC, t = threadIdx.x / TC, x = blockIdx.x * TC + c;
     float2 v[E];
 #pragma unroll
@@ -197,8 +205,9 @@ __global__ void k_abs2_sum(const float2 *__restrict__ S, int nn, double *out) {
     block_sum_doubles(a, 1, out);
 }
 
-// c_S = g * S (the cotangent of g/2 * sum |S|^2), c_P = 0.
-__global__ void k_seed_cotangent(const float2 *__restrict__ S, float2 *cP, float2 *cS, int nn, float g) {
+// c_S = g * S (the cotangent of g/2 * sum |S|^2), c_P = 0; g read from device memory.
+__global__ void k_seed_cotangent(const float2 *__restrict__ S, float2 *cP, float2 *cS, int nn, const double *gd) {
+    const float g = (float)*gd;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += gridDim.x * blockDim.x) {
         const float2 v = S[i];
         cS[i] = make_float2(g * v.x, g * v.y);
@@ -224,24 +233,23 @@ cudaError_t launch_rk4_vjp(const float2 *P0, const float2 *S0, float2 *cP, float
 }
 
 template <int N>
-static cudaError_t launch_colpass_t(int mode, float2 *A, const float2 *H, float2 *F, const InstDesc *d, double *acc,
-                                    cudaStream_t st) {
+static cudaError_t launch_colpass_t(int mode, float2 *A, float2 *F, const InstDesc *d, double *acc, cudaStream_t st) {
     constexpr int G = LineShape<N>::G, TC = 16;
+    const dim3 grid(N / TC, 2);
     if (mode == 0)
-        k_colpass<N, 0><<<N / TC, TC * G, 0, st>>>(A, H, F, d, acc);
+        k_colpass<N, 0><<<grid, TC * G, 0, st>>>(A, F, d, acc);
     else
-        k_colpass<N, 1><<<N / TC, TC * G, 0, st>>>(A, H, F, d, acc);
+        k_colpass<N, 1><<<grid, TC * G, 0, st>>>(A, F, d, acc);
     return cudaGetLastError();
 }
 
-cudaError_t launch_colpass(int n, int mode, float2 *A, const float2 *H, float2 *F, const InstDesc *d, double *acc,
-                           cudaStream_t st) {
+cudaError_t launch_colpass(int n, int mode, float2 *A, float2 *F, const InstDesc *d, double *acc, cudaStream_t st) {
     switch (n) {
-        case 16: return launch_colpass_t<16>(mode, A, H, F, d, acc, st);
-        case 32: return launch_colpass_t<32>(mode, A, H, F, d, acc, st);
-        case 64: return launch_colpass_t<64>(mode, A, H, F, d, acc, st);
-        case 128: return launch_colpass_t<128>(mode, A, H, F, d, acc, st);
-        case 256: return launch_colpass_t<256>(mode, A, H, F, d, acc, st);
+        case 16: return launch_colpass_t<16>(mode, A, F, d, acc, st);
+        case 32: return launch_colpass_t<32>(mode, A, F, d, acc, st);
+        case 64: return launch_colpass_t<64>(mode, A, F, d, acc, st);
+        case 128: return launch_colpass_t<128>(mode, A, F, d, acc, st);
+        case 256: return launch_colpass_t<256>(mode, A, F, d, acc, st);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -251,7 +259,7 @@ cudaError_t launch_abs2_sum(const float2 *S, int nn, double *out, cudaStream_t s
     return cudaGetLastError();
 }
 
-cudaError_t launch_seed_cotangent(const float2 *S, float2 *cP, float2 *cS, int nn, float g, cudaStream_t st) {
+cudaError_t launch_seed_cotangent(const float2 *S, float2 *cP, float2 *cS, int nn, const double *g, cudaStream_t st) {
     k_seed_cotangent<<<grid_for(nn), 256, 0, st>>>(S, cP, cS, nn, g);
     return cudaGetLastError();
 }

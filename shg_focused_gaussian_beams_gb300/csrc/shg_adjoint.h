@@ -12,10 +12,9 @@ cudaError_t launch_rk4_state(float2 *P, float2 *S, int nn, const float4 *stepc, 
                              cudaStream_t st);
 cudaError_t launch_rk4_vjp(const float2 *P0, const float2 *S0, float2 *cP, float2 *cS, int nn, const float4 *stepc,
                            int s, const InstDesc *d, double *acc_step, cudaStream_t st);
-cudaError_t launch_colpass(int n, int mode, float2 *A, const float2 *H, float2 *F, const InstDesc *d, double *acc,
-                           cudaStream_t st);
+cudaError_t launch_colpass(int n, int mode, float2 *A, float2 *F, const InstDesc *d, double *acc, cudaStream_t st);
 cudaError_t launch_abs2_sum(const float2 *S, int nn, double *out, cudaStream_t st);
-cudaError_t launch_seed_cotangent(const float2 *S, float2 *cP, float2 *cS, int nn, float g, cudaStream_t st);
+cudaError_t launch_seed_cotangent(const float2 *S, float2 *cP, float2 *cS, int nn, const double *g, cudaStream_t st);
 
 // Device work space of one gradient pass.
 struct AdjointWork {
@@ -23,6 +22,9 @@ struct AdjointWork {
     int ensure(int n, int K, int L, int nck);
     void release();
     int n = 0, K = 0, L = 0, nck = 0;
+    cudaGraphExec_t graph = nullptr;  // the captured gradient pass for (n, K, L) and graph_key
+    cudaStream_t cap = nullptr;       // capture stream
+    const void *graph_key[4] = {};    // device descriptor, P, S, step constants it was captured on
     void *mem = nullptr;
     size_t bytes = 0;
     float2 *X = nullptr, *cot = nullptr, *ck = nullptr, *Xs = nullptr, *Ws = nullptr, *Fs = nullptr;

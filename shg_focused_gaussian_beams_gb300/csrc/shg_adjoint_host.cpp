@@ -32,14 +32,23 @@ namespace shg {
         }                                                                                              \
     } while (0)
 
-AdjointWork::~AdjointWork() { release(); }
+AdjointWork::~AdjointWork() {
+    release();
+    if (cap) cudaStreamDestroy(cap);
+}
 
 void AdjointWork::release() {
+    if (graph) cudaGraphExecDestroy(graph);
+    graph = nullptr;
+    for (auto &k : graph_key) k = nullptr;
     if (mem) cudaFree(mem);
     mem = nullptr;
     bytes = 0;
 }
 
+// Layout: X, cot (one state each: P then S), nck checkpoint states, and L segment states
+// for each of X_s, W_s, F_s; then per-step sums (K x 8 doubles) and 8 global doubles
+// ([0..1] propagator sums, [2] sum |S_out|^2, [3] seed scale).
 int AdjointWork::ensure(int n_, int K_, int L_, int nck_) {
     if (mem && n == n_ && K == K_ && L == L_ && nck == nck_) return SHG_OK;
     release();
@@ -48,9 +57,7 @@ int AdjointWork::ensure(int n_, int K_, int L_, int nck_) {
     L = L_;
     nck = nck_;
     const size_t nn = (size_t)n * n;
-    const size_t st = 2 * nn;  // one state: P then S
-    // X (2 fields), cot (2), checkpoints (nck states), segment X_s, W_s, F_s (L states each),
-    // per-step sums (K x 8 doubles), propagator sums + loss (8 doubles)
+    const size_t st = 2 * nn;
     bytes = sizeof(float2) * (st * (2 + (size_t)nck + 3 * (size_t)L)) + sizeof(double) * (8 * (size_t)K + 8);
     AD_CUDA(cudaMalloc(&mem, bytes));
     float2 *p = reinterpret_cast<float2 *>(mem);
@@ -85,32 +92,20 @@ static double sellmeier_dT(double L, double T) {
     return dn2 / (2 * std::sqrt(n2));
 }
 
-static int rows2(int n, int sign, float2 *A, cudaStream_t st) {
-    const size_t nn = (size_t)n * n;
-    AD_CUDA(launch_dft_rows(n, sign, A, A, st));
-    AD_CUDA(launch_dft_rows(n, sign, A + nn, A + nn, st));
+// X <- D(X) for both fields (stored back to back); spectra into F when F != nullptr.
+static int diffraction_fwd(int n, float2 *X, float2 *F, const InstDesc *d, cudaStream_t st) {
+    AD_CUDA(launch_dft_rows(n, +1, X, X, st, 2));
+    AD_CUDA(launch_colpass(n, 0, X, F, d, nullptr, st));
+    AD_CUDA(launch_dft_rows(n, -1, X, X, st, 2));
     return SHG_OK;
 }
 
-// X <- D(X) (both fields); spectra stored in F (2 fields) when F != nullptr.
-static int diffraction_fwd(int n, float2 *X, float2 *F, const InstDesc &h, const InstDesc *d, cudaStream_t st) {
-    const size_t nn = (size_t)n * n;
-    int rc = rows2(n, +1, X, st);
-    if (rc) return rc;
-    AD_CUDA(launch_colpass(n, 0, X, h.Hp, F, d, nullptr, st));
-    AD_CUDA(launch_colpass(n, 0, X + nn, h.Hs, F ? F + nn : nullptr, d, nullptr, st));
-    return rows2(n, -1, X, st);
-}
-
-// c <- D^H(c) with the propagator sensitivities added to acc[0], acc[1].
-static int diffraction_adj(int n, float2 *c, float2 *F, const InstDesc &h, const InstDesc *d, double *acc,
-                           cudaStream_t st) {
-    const size_t nn = (size_t)n * n;
-    int rc = rows2(n, +1, c, st);
-    if (rc) return rc;
-    AD_CUDA(launch_colpass(n, 1, c, h.Hp, F, d, acc + 0, st));
-    AD_CUDA(launch_colpass(n, 1, c + nn, h.Hs, F + nn, d, acc + 1, st));
-    return rows2(n, -1, c, st);
+// c <- D^H(c) for both fields, propagator sensitivities added to acc[0], acc[1].
+static int diffraction_adj(int n, float2 *c, float2 *F, const InstDesc *d, double *acc, cudaStream_t st) {
+    AD_CUDA(launch_dft_rows(n, +1, c, c, st, 2));
+    AD_CUDA(launch_colpass(n, 1, c, F, d, acc, st));
+    AD_CUDA(launch_dft_rows(n, -1, c, c, st, 2));
+    return SHG_OK;
 }
 
 static int rk4_state(int n, float2 *X, const InstDesc &h, const InstDesc *d, int s, cudaStream_t st) {
@@ -119,54 +114,100 @@ static int rk4_state(int n, float2 *X, const InstDesc &h, const InstDesc *d, int
     return SHG_OK;
 }
 
-int adjoint_run(const shg_config &cfg, const InstDesc &h, const InstDesc *d, float temp, int checkpoints,
-                AdjointWork &w, cudaStream_t st, float2 *grad_pump, float2 *grad_sh, double *out) {
+// The whole gradient pass on `st`, from the input fields in h.P / h.S to the cotangent of
+// the inputs in w.cot and the sums in w.acc_step / w.acc_glob (seed scale read from
+// w.acc_glob[3]). Segments of L steps; with L == 1 and as many checkpoints as steps the
+// forward pass keeps every step's X_s, W_s, F_s and the backward pass needs no replay.
+static int enqueue_pass(const InstDesc &h, const InstDesc *d, AdjointWork &w, int L, int nseg, bool store_all,
+                        cudaStream_t st) {
     const int n = h.n, K = h.nsteps;
     const size_t nn = (size_t)n * n, sb = 2 * nn * sizeof(float2);
-    if (checkpoints < 1) checkpoints = 1;
-    if (checkpoints > K) checkpoints = K;
-    const int L = (K + checkpoints - 1) / checkpoints;
-    const int nseg = (K + L - 1) / L;
-    int rc = w.ensure(n, K, L, nseg);
-    if (rc) return rc;
-    AD_CUDA(cudaMemsetAsync(w.acc_step, 0, sizeof(double) * (8 * (size_t)K + 8), st));
-    // P and S of the solve hold the input fields after the set-up.
+    int rc;
+    AD_CUDA(cudaMemsetAsync(w.acc_step, 0, sizeof(double) * (8 * (size_t)K + 3), st));
     AD_CUDA(cudaMemcpyAsync(w.X, h.P, nn * sizeof(float2), cudaMemcpyDeviceToDevice, st));
     AD_CUDA(cudaMemcpyAsync(w.X + nn, h.S, nn * sizeof(float2), cudaMemcpyDeviceToDevice, st));
-    // forward with checkpoints
+    // forward: checkpoints every L steps (store_all: X_s, W_s, F_s of every step)
     for (int s = 0; s < K; ++s) {
-        if (s % L == 0) AD_CUDA(cudaMemcpyAsync(w.ck + (size_t)(s / L) * 2 * nn, w.X, sb, cudaMemcpyDeviceToDevice, st));
-        if ((rc = rk4_state(n, w.X, h, d, s, st))) return rc;
-        if ((rc = diffraction_fwd(n, w.X, nullptr, h, d, st))) return rc;
-        if ((rc = rk4_state(n, w.X, h, d, s, st))) return rc;
-    }
-    // loss: P_SH = 1/2 eps0 c n_s dx dy sum |S_out|^2
-    double *lsum = w.acc_glob + 2;
-    AD_CUDA(launch_abs2_sum(w.X + nn, (int)nn, lsum, st));
-    const float lp = cfg.lp, ls = (float)(0.5 * (double)lp);
-    const float ns = sellmeier(ls, temp), np = sellmeier(lp, temp);
-    const double kl = field_power(1.0, ns, h.dx, h.dy);
-    AD_CUDA(launch_seed_cotangent(w.X + nn, w.cot, w.cot + nn, (int)nn, (float)(2.0 * kl), st));
-    // backward
-    for (int seg = nseg - 1; seg >= 0; --seg) {
-        const int s0 = seg * L, s1 = std::min(K, s0 + L);
-        AD_CUDA(cudaMemcpyAsync(w.X, w.ck + (size_t)seg * 2 * nn, sb, cudaMemcpyDeviceToDevice, st));
-        for (int s = s0; s < s1; ++s) {
-            const size_t j = (size_t)(s - s0) * 2 * nn;
+        if (store_all) {
+            const size_t j = (size_t)s * 2 * nn;
             AD_CUDA(cudaMemcpyAsync(w.Xs + j, w.X, sb, cudaMemcpyDeviceToDevice, st));
             if ((rc = rk4_state(n, w.X, h, d, s, st))) return rc;
-            if ((rc = diffraction_fwd(n, w.X, w.Fs + j, h, d, st))) return rc;
+            if ((rc = diffraction_fwd(n, w.X, w.Fs + j, d, st))) return rc;
             AD_CUDA(cudaMemcpyAsync(w.Ws + j, w.X, sb, cudaMemcpyDeviceToDevice, st));
             if ((rc = rk4_state(n, w.X, h, d, s, st))) return rc;
+            continue;
+        }
+        if (s % L == 0) AD_CUDA(cudaMemcpyAsync(w.ck + (size_t)(s / L) * 2 * nn, w.X, sb, cudaMemcpyDeviceToDevice, st));
+        if ((rc = rk4_state(n, w.X, h, d, s, st))) return rc;
+        if ((rc = diffraction_fwd(n, w.X, nullptr, d, st))) return rc;
+        if ((rc = rk4_state(n, w.X, h, d, s, st))) return rc;
+    }
+    AD_CUDA(launch_abs2_sum(w.X + nn, (int)nn, w.acc_glob + 2, st));
+    AD_CUDA(launch_seed_cotangent(w.X + nn, w.cot, w.cot + nn, (int)nn, w.acc_glob + 3, st));
+    // backward
+    for (int seg = nseg - 1; seg >= 0; --seg) {
+        const int s0 = store_all ? 0 : seg * L, s1 = store_all ? K : std::min(K, s0 + L);
+        if (!store_all) {
+            AD_CUDA(cudaMemcpyAsync(w.X, w.ck + (size_t)seg * 2 * nn, sb, cudaMemcpyDeviceToDevice, st));
+            for (int s = s0; s < s1; ++s) {
+                const size_t j = (size_t)(s - s0) * 2 * nn;
+                AD_CUDA(cudaMemcpyAsync(w.Xs + j, w.X, sb, cudaMemcpyDeviceToDevice, st));
+                if ((rc = rk4_state(n, w.X, h, d, s, st))) return rc;
+                if ((rc = diffraction_fwd(n, w.X, w.Fs + j, d, st))) return rc;
+                AD_CUDA(cudaMemcpyAsync(w.Ws + j, w.X, sb, cudaMemcpyDeviceToDevice, st));
+                if ((rc = rk4_state(n, w.X, h, d, s, st))) return rc;
+            }
         }
         for (int s = s1 - 1; s >= s0; --s) {
             const size_t j = (size_t)(s - s0) * 2 * nn;
             double *as = w.acc_step + 8 * (size_t)s;
             AD_CUDA(launch_rk4_vjp(w.Ws + j, w.Ws + j + nn, w.cot, w.cot + nn, (int)nn, h.stepc, s, d, as, st));
-            if ((rc = diffraction_adj(n, w.cot, w.Fs + j, h, d, w.acc_glob, st))) return rc;
+            if ((rc = diffraction_adj(n, w.cot, w.Fs + j, d, w.acc_glob, st))) return rc;
             AD_CUDA(launch_rk4_vjp(w.Xs + j, w.Xs + j + nn, w.cot, w.cot + nn, (int)nn, h.stepc, s, d, as, st));
         }
+        if (store_all) break;
     }
+    return SHG_OK;
+}
+
+int adjoint_run(const shg_config &cfg, const InstDesc &h, const InstDesc *d, float temp, int checkpoints,
+                AdjointWork &w, cudaStream_t st, float2 *grad_pump, float2 *grad_sh, double *out) {
+    const int n = h.n, K = h.nsteps;
+    const size_t nn = (size_t)n * n;
+    if (checkpoints < 1) checkpoints = 1;
+    const bool store_all = checkpoints >= K;
+    if (checkpoints > K) checkpoints = K;
+    const int L = store_all ? K : (K + checkpoints - 1) / checkpoints;
+    const int nseg = store_all ? 1 : (K + L - 1) / L;
+    int rc = w.ensure(n, K, L, store_all ? 0 : nseg);
+    if (rc) return rc;
+    // loss scale: P_SH = 1/2 eps0 c n_s dx dy sum |S_out|^2; the seed is 2 * that scale
+    const float lp = cfg.lp, ls = (float)(0.5 * (double)lp);
+    const float ns = sellmeier(ls, temp), np = sellmeier(lp, temp);
+    const double kl = field_power(1.0, ns, h.dx, h.dy);
+    const double seed = 2.0 * kl;
+    AD_CUDA(cudaMemcpyAsync(w.acc_glob + 3, &seed, sizeof(double), cudaMemcpyHostToDevice, st));
+    // the pass is captured once per (grid, steps, segments, solve) and replayed
+    const void *key[4] = {d, h.P, h.S, h.stepc};
+    if (!w.graph || std::memcmp(key, w.graph_key, sizeof(key)) != 0) {
+        if (w.graph) cudaGraphExecDestroy(w.graph);
+        w.graph = nullptr;
+        if (!w.cap) AD_CUDA(cudaStreamCreateWithFlags(&w.cap, cudaStreamNonBlocking));
+        cudaGraph_t g = nullptr;
+        AD_CUDA(cudaStreamBeginCapture(w.cap, cudaStreamCaptureModeThreadLocal));
+        rc = enqueue_pass(h, d, w, L, nseg, store_all, w.cap);
+        cudaError_t e = cudaStreamEndCapture(w.cap, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        AD_CUDA(e);
+        e = cudaGraphInstantiate(&w.graph, g, 0);
+        cudaGraphDestroy(g);
+        AD_CUDA(e);
+        std::memcpy(w.graph_key, key, sizeof(key));
+    }
+    AD_CUDA(cudaGraphLaunch(w.graph, st));
     if (grad_pump) AD_CUDA(cudaMemcpyAsync(grad_pump, w.cot, nn * sizeof(float2), cudaMemcpyDeviceToDevice, st));
     if (grad_sh) AD_CUDA(cudaMemcpyAsync(grad_sh, w.cot + nn, nn * sizeof(float2), cudaMemcpyDeviceToDevice, st));
     // parameter gradients on the host

@@ -29,7 +29,7 @@ cudaError_t launch_rows(int n, const InstDesc *inst, const int *list, int count,
 cudaError_t launch_cols(int n, const InstDesc *inst, const int *list, int count, cudaStream_t st);
 bool line_length_supported(int n);
 cudaError_t launch_dft2d(int n, int sign, const float2 *in, float2 *out, cudaStream_t st);
-cudaError_t launch_dft_rows(int n, int sign, const float2 *in, float2 *out, cudaStream_t st);
+cudaError_t launch_dft_rows(int n, int sign, const float2 *in, float2 *out, cudaStream_t st, int fields = 1);
 
 // shg_thermal.cu
 struct HeatCoef;

@@ -271,21 +271,22 @@ static cudaError_t launch_dft2d_t(int sign, const float2 *in, float2 *out, cudaS
 }
 
 template <int N>
-static cudaError_t launch_dft_rows_t(int sign, const float2 *in, float2 *out, cudaStream_t st) {
+static cudaError_t launch_dft_rows_t(int sign, const float2 *in, float2 *out, int fields, cudaStream_t st) {
+    const int blocks = RowShape<N>::BPI * fields;  // fields stored back to back: n*fields rows
     if (sign < 0)
-        k_dft_rows<N, -1><<<RowShape<N>::BPI, RowShape<N>::TPB, 0, st>>>(in, out);
+        k_dft_rows<N, -1><<<blocks, RowShape<N>::TPB, 0, st>>>(in, out);
     else
-        k_dft_rows<N, +1><<<RowShape<N>::BPI, RowShape<N>::TPB, 0, st>>>(in, out);
+        k_dft_rows<N, +1><<<blocks, RowShape<N>::TPB, 0, st>>>(in, out);
     return cudaGetLastError();
 }
 
-cudaError_t launch_dft_rows(int n, int sign, const float2 *in, float2 *out, cudaStream_t st) {
+cudaError_t launch_dft_rows(int n, int sign, const float2 *in, float2 *out, cudaStream_t st, int fields) {
     switch (n) {
-        case 16: return launch_dft_rows_t<16>(sign, in, out, st);
-        case 32: return launch_dft_rows_t<32>(sign, in, out, st);
-        case 64: return launch_dft_rows_t<64>(sign, in, out, st);
-        case 128: return launch_dft_rows_t<128>(sign, in, out, st);
-        case 256: return launch_dft_rows_t<256>(sign, in, out, st);
+        case 16: return launch_dft_rows_t<16>(sign, in, out, fields, st);
+        case 32: return launch_dft_rows_t<32>(sign, in, out, fields, st);
+        case 64: return launch_dft_rows_t<64>(sign, in, out, fields, st);
+        case 128: return launch_dft_rows_t<128>(sign, in, out, fields, st);
+        case 256: return launch_dft_rows_t<256>(sign, in, out, fields, st);
         default: return cudaErrorInvalidValue;
     }
 }

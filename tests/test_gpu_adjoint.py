@@ -7,6 +7,7 @@ point and varies with T and the poling period as the double-precision model does
 Bar: agreement to 1e-3 (relative).
 """
 import math
+import os
 
 import numpy as np
 import pytest
@@ -100,12 +101,29 @@ def test_poling_period_gradient_vs_fd(case):
     assert abs(case["r"]["dLambda"] - fd) / abs(fd) < FD_RTOL, (case["r"]["dLambda"], fd)
 
 
-def test_checkpoint_count_does_not_change_the_gradient(case):
-    r2 = case["s"].grad(T0, torch.from_numpy(case["pump64"].astype(np.complex64)).cuda(), checkpoints=NZ - 1)
+@pytest.mark.parametrize("checkpoints", [1, 3, NZ - 1])
+def test_checkpoint_count_does_not_change_the_gradient(case, checkpoints):
+    """One segment (full replay), a few segments, and every step stored (no replay)."""
+    r2 = case["s"].grad(T0, torch.from_numpy(case["pump64"].astype(np.complex64)).cuda(), checkpoints=checkpoints)
     g1 = case["r"]["grad_pump"].cpu().numpy()
     g2 = r2["grad_pump"].cpu().numpy()
     assert np.linalg.norm(g1 - g2) / np.linalg.norm(g1) < 1e-5
     assert abs(r2["dT"] - case["r"]["dT"]) / abs(case["r"]["dT"]) < 1e-5
+    assert abs(r2["loss"] - case["r"]["loss"]) / case["r"]["loss"] < 1e-6
+
+
+def test_graph_replay_with_new_input(case):
+    """The captured gradient pass is reused across calls: a different pump in between must
+    not leak into the next result."""
+    s = case["s"]
+    p = torch.from_numpy(case["pump64"].astype(np.complex64)).cuda()
+    ra = s.grad(T0, p, checkpoints=7)
+    rb = s.grad(T0, 0.5 * p, checkpoints=7)
+    rc = s.grad(T0, p, checkpoints=7)
+    assert rb["loss"] < 0.5 * ra["loss"]
+    np.testing.assert_allclose(rc["grad_pump"].cpu().numpy(), ra["grad_pump"].cpu().numpy(), rtol=0, atol=0)
+    # parameter sums are FP64 atomics (order-dependent in the last bits)
+    assert abs(rc["loss"] - ra["loss"]) <= 1e-12 * ra["loss"] and abs(rc["dT"] - ra["dT"]) <= 1e-12 * abs(ra["dT"])
 
 
 def test_autograd_focus_and_temperature(case):
@@ -124,3 +142,62 @@ def test_autograd_focus_and_temperature(case):
     fd = (Lp - Lm) / (2 * h)
     assert abs(focal.grad.item() - fd) / abs(fd) < FD_RTOL, (focal.grad.item(), fd)
     assert abs(temp.grad.item() - case["r"]["dT"]) / abs(case["r"]["dT"]) < 1e-6
+
+
+def _fd_job(args):
+    """One FP64 loss evaluation of the full-size case in a separate process."""
+    import oracle as Ox
+    cfg_t, pump, T, dk = args
+    o = Ox.Oracle(Ox.Cfg(*cfg_t))
+    _, so, _, _ = o.cwes_plain64(pump, np.zeros_like(pump), T, dk)
+    return float(np.sum(np.abs(so) ** 2)) * o.n64(0.532, T)
+
+
+def test_config_adjoint_256x400_full_size():
+    """The adjoint workload at full size: 256x256x400, P = 20 W, xi = 2.84, Gaussian pump
+    times a seeded 5 % perturbation smooth over 8 cells, 20 checkpoints; FP64 central
+    differences (run in parallel processes) on 4 field directions, T and Lambda."""
+    import multiprocessing as mpx
+    n, nz = 256, 400
+    inst = W.plain_instance(n, nz, 20.0, 2.84, T0)
+    cfg = O.make_cfg(W.CRYSTAL_QPM50, n, n, nz, inst.lx, inst.ly)
+    o = O.Oracle(cfg)
+    rng = np.random.default_rng(12)
+    pump = o.set_pump64(inst.power, inst.focal, inst.waist, T0) * (1 + 0.05 * smooth_noise(rng, n))
+    s = Solver(crystal=W.CRYSTAL_QPM50, nx=n, ny=n, nz=nz, lx=inst.lx, ly=inst.ly)
+    r = s.grad(T0, torch.from_numpy(pump.astype(np.complex64)).cuda(), checkpoints=20)
+    g = r["grad_pump"].cpu().numpy().astype(np.complex128)
+    dk32 = float(o.dk_constant(T0))
+    lam = cfg.lambda_qpm
+    cfg_t = tuple(getattr(cfg, f) for f, _ in O.Cfg._fields_)
+    eps0 = float(np.float32(8.8541878128e-12 * 1e12 / 1e6))
+    cl = float(np.float32(299792458 * 1e6 / 1e12))
+    kl = 0.5 * eps0 * cl * float(np.float32(inst.lx / (n - 1))) * float(np.float32(inst.ly / (n - 1)))
+    dirs = [smooth_noise(rng, n) * pump for _ in range(4)]
+    jobs, meta = [], []
+    for d in dirs:
+        eps = 1e-4 * np.linalg.norm(pump) / np.linalg.norm(d)
+        jobs += [(cfg_t, pump + eps * d, T0, dk32), (cfg_t, pump - eps * d, T0, dk32)]
+        meta.append(("field", 2 * eps, d))
+    hT = 1e-4 * T0
+    for sgn in (1, -1):
+        jobs.append((cfg_t, pump, T0 + sgn * hT, dk32 + o.dk_constant64(T0 + sgn * hT) - o.dk_constant64(T0)))
+    meta.append(("T", 2 * hT, None))
+    hL = 1e-7 * lam
+    for sgn in (1, -1):
+        jobs.append((cfg_t, pump, T0, dk32 + 2 * math.pi * (1.0 / (lam + sgn * hL) - 1.0 / lam)))
+    meta.append(("L", 2 * hL, None))
+    with mpx.get_context("spawn").Pool(min(len(jobs), os.cpu_count() or 1)) as pool:
+        vals = [kl * v for v in pool.map(_fd_job, jobs)]
+    adj, fd = [], []
+    for k, (kind, h, d) in enumerate(meta):
+        fdk = (vals[2 * k] - vals[2 * k + 1]) / h
+        if kind == "field":
+            adj.append(float(np.sum(np.real(np.conj(g) * d))))
+            fd.append(fdk)
+        elif kind == "T":
+            assert abs(r["dT"] - fdk) / abs(fdk) < FD_RTOL, (r["dT"], fdk)
+        else:
+            assert abs(r["dLambda"] - fdk) / abs(fdk) < FD_RTOL, (r["dLambda"], fdk)
+    adj, fd = np.array(adj), np.array(fd)
+    assert np.linalg.norm(adj - fd) / np.linalg.norm(fd) < FD_RTOL, (adj, fd)
