@@ -179,6 +179,43 @@ int shg_batch_profile(shg_batch *b, shg_kernel_stat *stats, int max_stats, int *
 int shg_cwes_noalloc(const shg_config *cfg, float temp, const void *pump_in, const void *sh_in,
                      void *pump_out, void *sh_out, double *eta, void *stream);
 
+/* ---- Batched gradient of the THERMAL z-march (fixed temperature fields) ----------- */
+/* No counterpart in the reference (its THERMAL Solver::run, Solver.h:287-340, is forward
+ * only). `count` solves on one grid (cfg: NX = NY a power of two in [16, 256]; the
+ * crystal and heat constants as for a THERMAL handle), each with its own temperature field
+ * held fixed. Solve i's loss is its SH output power (the state at the top of slice NZ-1 of
+ * the THERMAL CWES, Solver.h:245-276, without heat-source updates); the gradient is taken
+ * with respect to its input pump, in the form dL/dRe + i dL/dIm. Propagators, the Gaussian
+ * reference pump and the power convention use n at T[NX/2, NY/2, 0] (Efields.h:77,110). */
+typedef struct shg_thgrad shg_thgrad;
+int shg_thgrad_create(const shg_config *cfg, int count, shg_thgrad **out);
+void shg_thgrad_destroy(shg_thgrad *b);
+/* Solver::run (THERMAL) for solve i with a Gaussian pump (Solver::run's arguments); its
+ * final temperature field is kept, and that pump becomes the solve's reference input.
+ * counts (5 ints, may be NULL) receives the Jacobi sweeps of each outer iteration. */
+int shg_thgrad_solve_temperature(shg_thgrad *b, int i, float power, float waist, float focal, float temp,
+                                 float t_inf, float t1, float t2, int *counts);
+/* Solve i's temperature field given directly (host, NX*NY*NZ floats, IDX(x,y,z)) and the
+ * Gaussian reference input of (power, waist, focal). */
+int shg_thgrad_set_temperature(shg_thgrad *b, int i, const float *T, float power, float waist, float focal);
+int shg_thgrad_get_temperature(shg_thgrad *b, int i, float *T);
+/* The solves' Gaussian reference inputs into a device buffer of count*NX*NY complex64. */
+int shg_thgrad_gaussian_pumps(shg_thgrad *b, void *pump, void *stream);
+/* Forward pass of every solve: pump_in (device, count*NX*NY complex64, solve-major), SH
+ * start zero; pump_out / sh_out (device, may be NULL) receive the output fields; p_sh /
+ * p_in (host, count doubles, may be NULL; the call then synchronises `stream`) the SH
+ * output power and the input pump power [W]. */
+int shg_thgrad_forward(shg_thgrad *b, const void *pump_in, void *pump_out, void *sh_out, double *p_sh, double *p_in,
+                       void *stream);
+/* Forward and reverse pass: grad_pump (device, count*NX*NY) = dP_SH,i / dA_in,i.
+ * checkpoints < NZ-1 keeps that many states per solve and replays segments; checkpoints
+ * >= NZ-1 keeps every step (no replay; 2*(NZ-1) states per solve). */
+int shg_thgrad_gradient(shg_thgrad *b, const void *pump_in, int checkpoints, void *grad_pump, double *p_sh,
+                        double *p_in, void *stream);
+/* Kernel launches of the last forward or gradient pass; device memory held. */
+int shg_thgrad_launch_count(const shg_thgrad *b);
+double shg_thgrad_device_bytes(const shg_thgrad *b);
+
 /* ---- Components, for tests ------------------------------------------------------- */
 /* Unnormalised 2D DFT of an n x n complex array on the device (sign -1 forward, +1
  * backward, FFTW's convention), device pointers, in place allowed. */

@@ -64,6 +64,8 @@ def lib():
         L.oracle_reduced_sum.argtypes = [P, _pf, _pf]
         L.oracle_dk_thermal.argtypes = [P, _pf, _pf]
         L.oracle_set_q.argtypes = [P, _pf, _pf, _pf, _i, _pf]
+        L.oracle_cwes_thermal_f32.argtypes = [P, _pf, _pf, _pf, _pf, _f, _pf, _pf]
+        L.oracle_cwes_thermal_f64.argtypes = [P, _pd, _pd, _pd, _pd, _d, _pd, _pd]
         L.oracle_thermal_run.restype = _i
         L.oracle_thermal_run.argtypes = [P, _f, _f, _f, _f, _f, _f, _f, _i, _i, _pf, _pf, _pf, _pi]
         L.oracle_sweep_plain.argtypes = [P, C.POINTER(Inst), _i, _i, _pd]
@@ -186,6 +188,26 @@ class Oracle:
                             _pF(np.ascontiguousarray(pump, np.complex64)),
                             _pF(np.ascontiguousarray(sh, np.complex64)), s, _pF(Qn))
         return Qn
+
+    def cwes_thermal(self, T, pump, sh, tc, dk3=None):
+        """THERMAL CWES with T held fixed (float); returns the fields at the top of slice NZ-1."""
+        Tn = np.ascontiguousarray(T, np.float32)
+        dk = None if dk3 is None else np.ascontiguousarray(dk3, np.float32)
+        po, so = self._c2(), self._c2()
+        self.L.oracle_cwes_thermal_f32(C.byref(self.cfg), _pF(Tn), _pF(dk) if dk is not None else None,
+                                       _pF(np.ascontiguousarray(pump, np.complex64)),
+                                       _pF(np.ascontiguousarray(sh, np.complex64)), tc, _pF(po), _pF(so))
+        return po, so
+
+    def cwes_thermal64(self, T, pump, sh, tc, dk3=None):
+        """Same in double; dk3 (e.g. the float delta-k table) pins delta-k."""
+        Tn = np.ascontiguousarray(T, np.float64)
+        dk = None if dk3 is None else np.ascontiguousarray(dk3, np.float64)
+        po, so = self._c2(np.complex128), self._c2(np.complex128)
+        self.L.oracle_cwes_thermal_f64(C.byref(self.cfg), _pD(Tn), _pD(dk) if dk is not None else None,
+                                       _pD(np.ascontiguousarray(pump, np.complex128)),
+                                       _pD(np.ascontiguousarray(sh, np.complex128)), tc, _pD(po), _pD(so))
+        return po, so
 
     def thermal_run(self, power, waist, focal, temp, t_inf, t1, t2, bc=0, sh_seed=-1):
         po, so = self._c2(), self._c2()

@@ -499,10 +499,11 @@ float reduced_sum(const Model<float> &m, const float *Tf, const float *Ti) {
 }
 
 // PhaseMatching.h:41-54
-void dk_thermal(const Model<float> &m, const float *T, float *DK) {
-    const float PI = m.PI;
+template <class R>
+void dk_thermal(const Model<R> &m, const R *T, R *DK) {
+    const R PI = m.PI;
     for (size_t i = 0; i < m.TSIZE; ++i)
-        DK[i] = 2 * PI * (2 * m.n(m.lp, T[i]) / m.lp - m.n(m.ls, T[i]) / m.ls + 1 / (m.Lambda));
+        DK[i] = (R)2 * PI * ((R)2 * m.n(m.lp, T[i]) / m.lp - m.n(m.ls, T[i]) / m.ls + (R)1 / (m.Lambda));
 }
 
 template <class R>
@@ -516,6 +517,24 @@ template <class R>
 cx<R> *as_cx(R *p) { return reinterpret_cast<cx<R> *>(p); }
 template <class R>
 const cx<R> *as_cx(const R *p) { return reinterpret_cast<const cx<R> *>(p); }
+
+// Solver.h:245-276 (THERMAL) from given fields with the temperature field held fixed;
+// DK3 == nullptr: delta-k(T) in R, else the given table (to pin the float delta-k).
+template <class R>
+void cwes_thermal_impl(const oracle_cfg *c, const R *T, const R *DK3, const R *pump, const R *sh, R tc,
+                       R *out_pump, R *out_sh) {
+    Model<R> m(*c);
+    cvec<R> P(as_cx(pump), as_cx(pump) + m.NXY), S(as_cx(sh), as_cx(sh) + m.NXY);
+    cvec<R> hp(m.NXY), hs(m.NXY);
+    propagators<R>(m, tc, hp.data(), hs.data());
+    std::vector<R> dk(m.TSIZE), Q(m.TSIZE);
+    if (DK3)
+        std::copy(DK3, DK3 + m.TSIZE, dk.begin());
+    else
+        dk_thermal<R>(m, T, dk.data());
+    cwes<R>(m, P.data(), S.data(), hp.data(), hs.data(), true, (R)0, tc, T, dk.data(), Q.data(),
+            out_pump ? as_cx(out_pump) : nullptr, out_sh ? as_cx(out_sh) : nullptr);
+}
 
 template <class R>
 void cwes_plain_impl(const oracle_cfg *c, const R *pump, const R *sh, R temp, R dk, R *out_pump,
@@ -622,7 +641,16 @@ float oracle_reduced_sum(const oracle_cfg *c, const float *Tf, const float *Ti) 
 
 void oracle_dk_thermal(const oracle_cfg *c, const float *T, float *DK) {
     Model<float> m(*c);
-    dk_thermal(m, T, DK);
+    dk_thermal<float>(m, T, DK);
+}
+
+void oracle_cwes_thermal_f32(const oracle_cfg *c, const float *T, const float *DK3, const float *pump,
+                             const float *sh, float tc, float *out_pump, float *out_sh) {
+    cwes_thermal_impl<float>(c, T, DK3, pump, sh, tc, out_pump, out_sh);
+}
+void oracle_cwes_thermal_f64(const oracle_cfg *c, const double *T, const double *DK3, const double *pump,
+                             const double *sh, double tc, double *out_pump, double *out_sh) {
+    cwes_thermal_impl<double>(c, T, DK3, pump, sh, tc, out_pump, out_sh);
 }
 
 void oracle_set_q(const oracle_cfg *c, const float *T, const float *pump, const float *sh, int s, float *Q) {
@@ -657,7 +685,7 @@ int oracle_thermal_run(const oracle_cfg *c, float power, float waist, float foca
             counter_T++;
         }
         counts[outer++] = (int)counter_T;
-        dk_thermal(m, Tf.data(), DK.data());
+        dk_thermal<float>(m, Tf.data(), DK.data());
         const float tc = Tf[m.idx(m.NX / 2, m.NY / 2, 0)];
         set_pump<float>(m, power, focal, waist, tc, P.data());
         if (sh_seed >= 0)

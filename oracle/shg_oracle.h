@@ -73,6 +73,14 @@ void oracle_heat_sweeps(const oracle_cfg *c, float *T, const float *Q, float t_i
 float oracle_reduced_sum(const oracle_cfg *c, const float *Tf, const float *Ti);
 void oracle_dk_thermal(const oracle_cfg *c, const float *T, float *DK);
 void oracle_set_q(const oracle_cfg *c, const float *T, const float *pump, const float *sh, int s, float *Q);
+/* THERMAL CWES (Solver.h:245-276) from given fields with the temperature field T
+ * (NX*NY*NZ) held fixed: n from T per pixel, delta-k from DK3 (NULL: PhaseMatching.h:41-54
+ * evaluated in the function's precision), propagators at tc. out_*: state at the top of
+ * slice NZ-1. */
+void oracle_cwes_thermal_f32(const oracle_cfg *c, const float *T, const float *DK3, const float *pump,
+                             const float *sh, float tc, float *out_pump, float *out_sh);
+void oracle_cwes_thermal_f64(const oracle_cfg *c, const double *T, const double *DK3, const double *pump,
+                             const double *sh, double tc, double *out_pump, double *out_sh);
 /* Solver::run with THERMAL (Solver.h:287-340) as the reference drives it; counts[5]
  * receives the Jacobi sweeps of each outer iteration (-1 if not run). Returns the
  * number of outer iterations. */

@@ -77,6 +77,16 @@ SIGNATURES = {
     "shg_dk_thermal": (_i, [C.POINTER(Config), _pf, _pf, _pf, _pf]),
     "shg_heat_sweeps_device": (_i, [C.POINTER(Config), _vp, _vp, _vp, _f, _i, _i, _vp]),
     "shg_cwes_noalloc": (_i, [C.POINTER(Config), _f, _vp, _vp, _vp, _vp, _pd, _vp]),
+    "shg_thgrad_create": (_i, [C.POINTER(Config), _i, C.POINTER(_vp)]),
+    "shg_thgrad_destroy": (None, [_vp]),
+    "shg_thgrad_solve_temperature": (_i, [_vp, _i, _f, _f, _f, _f, _f, _f, _f, _pi]),
+    "shg_thgrad_set_temperature": (_i, [_vp, _i, _pf, _f, _f, _f]),
+    "shg_thgrad_get_temperature": (_i, [_vp, _i, _pf]),
+    "shg_thgrad_gaussian_pumps": (_i, [_vp, _vp, _vp]),
+    "shg_thgrad_forward": (_i, [_vp, _vp, _vp, _vp, _pd, _pd, _vp]),
+    "shg_thgrad_gradient": (_i, [_vp, _vp, _i, _vp, _pd, _pd, _vp]),
+    "shg_thgrad_launch_count": (_i, [_vp]),
+    "shg_thgrad_device_bytes": (C.c_double, [_vp]),
 }
 
 _lib = None

@@ -6,6 +6,9 @@ temperature (input fields held fixed) and the poling period through the hand-wri
 adjoint (``shg_grad_device``), with the checkpoint count of the solver wrapper. Build the
 pump with torch operations (e.g. ``gaussian_pump``) to carry gradients on to its own
 parameters (focus position, waist, power).
+
+``thermal_batch_power(batch, pumps)`` does the same for a batch of THERMAL solves whose
+temperature fields are held fixed (``shg_thgrad_gradient``), differentiable in the pumps.
 """
 from __future__ import annotations
 
@@ -46,6 +49,29 @@ def shg_power(solver, pump, temp, lambda_qpm, checkpoints=20):
     temp = torch.as_tensor(temp, dtype=torch.float64, device=pump.device)
     lam = torch.as_tensor(lambda_qpm, dtype=torch.float64, device=pump.device)
     return _SHGPower.apply(pump, temp, lam, solver, checkpoints)
+
+
+class _ThermalBatchPower(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, pump, batch, checkpoints):
+        p32 = pump.detach().to(torch.complex64).contiguous()
+        r = batch.gradient(p32, checkpoints=checkpoints)
+        ctx.save_for_backward(r["grad"])
+        ctx.pump_dtype = pump.dtype
+        return torch.as_tensor(r["p_sh"], dtype=torch.float64, device=pump.device)
+
+    @staticmethod
+    def backward(ctx, g):
+        (gp,) = ctx.saved_tensors
+        gpump = (g.to(torch.float32)[:, None, None] * gp).to(ctx.pump_dtype)
+        return gpump, None, None
+
+
+def thermal_batch_power(batch, pump, checkpoints=20):
+    """SH output powers (W, float64 tensor of shape (count,)) of a ThermalGradBatch for the
+    input pumps (count, NY, NX), differentiable in the pumps (temperature fields fixed).
+    The gradient pass runs with the forward call."""
+    return _ThermalBatchPower.apply(pump, batch, checkpoints)
 
 
 def gaussian_pump(nx, ny, lx, ly, power, waist, focal, temp, lp=1.064, dtype=torch.complex128, device="cuda"):

@@ -13,6 +13,7 @@
 // gradients (oven temperature, poling period) on the host.
 #include <cuda_runtime.h>
 
+#include "shg_adjoint.cuh"
 #include "shg_internal.h"
 #include "shg_march.cuh"
 
@@ -22,24 +23,6 @@ const float2 *twiddle_symbol_address_adjoint() {
     void *p = nullptr;
     cudaGetSymbolAddress(&p, g_twiddle);
     return static_cast<const float2 *>(p);
-}
-
-__device__ __forceinline__ void block_sum_doubles(double *v, int k, double *dst) {
-    __shared__ double red[32][6];
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    for (int j = 0; j < k; ++j)
-        for (int o = 16; o > 0; o >>= 1) v[j] += __shfl_xor_sync(0xffffffffu, v[j], o);
-    __syncthreads();
-    if (l == 0)
-        for (int j = 0; j < k; ++j) red[w][j] = v[j];
-    __syncthreads();
-    if (w == 0) {
-        for (int j = 0; j < k; ++j) {
-            double x = (l < (int)(blockDim.x >> 5)) ? red[l][j] : 0.0;
-            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-            if (l == 0 && x != 0.0) atomicAdd(dst + j, x);
-        }
-    }
 }
 
 // Forward RK4 on a plain state (Solver.h:216-228 with the step constants folded).
@@ -53,37 +36,6 @@ __global__ void k_rk4_state(float2 *P, float2 *S, int nn, const float4 *__restri
         P[i] = p;
         S[i] = q;
     }
-}
-
-// Reverse mode of one dA/dz evaluation at (P, S) with output cotangents (u, v); adds the
-// input cotangents to (cp, cs) and the parameter sensitivities to acc.
-__device__ __forceinline__ void dadz_vjp(float2 P, float2 S, float2 u, float2 v, float4 c, float hp, float tpa0,
-                                         float tpa1, float2 &cp, float2 &cs, double *acc) {
-    const float2 aP = make_float2(c.x, c.y), aS = make_float2(c.z, c.w);
-    // c_P = -hp u + aP S conj(u) + 2 conj(aS) conj(P) v
-    const float2 aPS = c_mul(aP, S);
-    const float2 t1 = c_mulc(aPS, u);                      // aP S conj(u)
-    const float2 cPv = c_mulc(v, c_mul(aS, P));            // v conj(aS P) = conj(aS) conj(P) v
-    cp.x += -hp * u.x + t1.x + 2.0f * cPv.x;
-    cp.y += -hp * u.y + t1.y + 2.0f * cPv.y;
-    // c_S = conj(aP) P u - (tpa0 + 2 tpa1 |S|^2) v - tpa1 S^2 conj(v)
-    const float a2 = fmaf(S.x, S.x, S.y * S.y);
-    const float2 t2 = c_mulc(c_mul(P, u), aP);             // P u conj(aP)
-    const float2 S2 = c_mul(S, S);
-    const float2 t3 = c_mulc(S2, v);                       // S^2 conj(v)
-    const float g = fmaf(2.0f * tpa1, a2, tpa0);
-    cs.x += t2.x - g * v.x - tpa1 * t3.x;
-    cs.y += t2.y - g * v.y - tpa1 * t3.y;
-    // sensitivities: sum conj(S conj(P)) u, sum conj(P^2) v, sum Re(conj(v) (-|S|^2 S))
-    const float2 gP = c_mulc(S, P);                        // S conj(P)
-    const float2 hS = c_mul(P, P);
-    const float2 eP = c_mulc(u, gP);                       // u conj(g)
-    const float2 eS = c_mulc(v, hS);                       // v conj(h)
-    acc[0] += (double)eP.x;
-    acc[1] += (double)eP.y;
-    acc[2] += (double)eS.x;
-    acc[3] += (double)eS.y;
-    acc[4] += -(double)a2 * ((double)v.x * S.x + (double)v.y * S.y);
 }
 
 // RK4^T at the base state (P0, S0): (cP, cS) hold the cotangent of the RK4 output on
@@ -147,20 +99,21 @@ __global__ void k_rk4_vjp(const float2 *__restrict__ P0, const float2 *__restric
 // where X is the transformed cotangent and q2 = dfX^2 tx^2 + dfY^2 ty^2 of the propagator
 // phase (Efields.h:121), so that acc * dz * g / k is the derivative of L w.r.t. the
 // wavenumber k = 2 pi n / lambda of that field.
-// Both fields in one launch: blockIdx.y = 0 pump (Hp), 1 SH (Hs); A and Fst hold the two
-// fields back to back, acc[field] receives the sums.
+//   MODE 2 (adjoint, no sums): multiply by conj(H'), forward.
+// All fields of all solves in one launch: blockIdx.y = 2*solve + {0 pump (Hp), 1 SH (Hs)};
+// A and Fst hold the fields back to back (solve-major), acc[blockIdx.y] receives the sums.
 template <int N, int MODE>
 __global__ void __launch_bounds__(16 * LineShape<N>::G) k_colpass(float2 *A0, float2 *Fst0,
                                                              const InstDesc *__restrict__ dd, double *acc0) {
     constexpr int G = LineShape<N>::G, E = N / G, TC = 16;
     __shared__ float2 scratch[TC * E * G];
     const float2 *__restrict__ tab = g_twiddle + N;
-    const InstDesc &d = *dd;
     const int f = blockIdx.y;
+    const InstDesc &d = dd[f >> 1];
     const size_t nn = (size_t)N * N;
     float2 *A = A0 + f * nn;
     float2 *Fst = Fst0 ? Fst0 + f * nn : nullptr;
-    const float2 *__restrict__ H = f == 0 ? d.Hp : d.Hs;
+    const float2 *__restrict__ H = (f & 1) ? d.Hs : d.Hp;
     double *acc = acc0 ? acc0 + f : nullptr;
     const int c = threadIdx.x % TC, t = threadIdx.x / TC, x = blockIdx.x * TC + c;
     float2 v[E];
@@ -176,6 +129,8 @@ __global__ void __launch_bounds__(16 * LineShape<N>::G) k_colpass(float2 *A0, fl
         if (MODE == 0) {
             if (Fst) Fst[i] = v[r];
             v[r] = c_mul(v[r], h);
+        } else if (MODE == 2) {
+            v[r] = c_mulc(v[r], h);
         } else {
             const int ux = (x + N / 2) & (N - 1), uy = (k + N / 2) & (N - 1);
             const float tx = (float)ux - d.uX, ty = (float)uy - d.uY;
@@ -233,23 +188,28 @@ cudaError_t launch_rk4_vjp(const float2 *P0, const float2 *S0, float2 *cP, float
 }
 
 template <int N>
-static cudaError_t launch_colpass_t(int mode, float2 *A, float2 *F, const InstDesc *d, double *acc, cudaStream_t st) {
+static cudaError_t launch_colpass_t(int mode, float2 *A, float2 *F, const InstDesc *d, double *acc, int solves,
+                                    cudaStream_t st) {
     constexpr int G = LineShape<N>::G, TC = 16;
-    const dim3 grid(N / TC, 2);
+    const dim3 grid(N / TC, 2 * solves);
     if (mode == 0)
         k_colpass<N, 0><<<grid, TC * G, 0, st>>>(A, F, d, acc);
-    else
+    else if (mode == 1)
         k_colpass<N, 1><<<grid, TC * G, 0, st>>>(A, F, d, acc);
+    else
+        k_colpass<N, 2><<<grid, TC * G, 0, st>>>(A, F, d, acc);
     return cudaGetLastError();
 }
 
-cudaError_t launch_colpass(int n, int mode, float2 *A, float2 *F, const InstDesc *d, double *acc, cudaStream_t st) {
+cudaError_t launch_colpass(int n, int mode, float2 *A, float2 *F, const InstDesc *d, double *acc, cudaStream_t st,
+                           int solves) {
+    if (solves < 1 || solves > 32767) return cudaErrorInvalidValue;
     switch (n) {
-        case 16: return launch_colpass_t<16>(mode, A, F, d, acc, st);
-        case 32: return launch_colpass_t<32>(mode, A, F, d, acc, st);
-        case 64: return launch_colpass_t<64>(mode, A, F, d, acc, st);
-        case 128: return launch_colpass_t<128>(mode, A, F, d, acc, st);
-        case 256: return launch_colpass_t<256>(mode, A, F, d, acc, st);
+        case 16: return launch_colpass_t<16>(mode, A, F, d, acc, solves, st);
+        case 32: return launch_colpass_t<32>(mode, A, F, d, acc, solves, st);
+        case 64: return launch_colpass_t<64>(mode, A, F, d, acc, solves, st);
+        case 128: return launch_colpass_t<128>(mode, A, F, d, acc, solves, st);
+        case 256: return launch_colpass_t<256>(mode, A, F, d, acc, solves, st);
         default: return cudaErrorInvalidValue;
     }
 }

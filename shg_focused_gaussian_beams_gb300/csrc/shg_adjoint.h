@@ -12,7 +12,11 @@ cudaError_t launch_rk4_state(float2 *P, float2 *S, int nn, const float4 *stepc, 
                              cudaStream_t st);
 cudaError_t launch_rk4_vjp(const float2 *P0, const float2 *S0, float2 *cP, float2 *cS, int nn, const float4 *stepc,
                            int s, const InstDesc *d, double *acc_step, cudaStream_t st);
-cudaError_t launch_colpass(int n, int mode, float2 *A, float2 *F, const InstDesc *d, double *acc, cudaStream_t st);
+// Column pass of the diffraction over `solves` solves (d[solves], fields solve-major):
+// mode 0 forward (spectra into F when F != nullptr), 1 adjoint with the propagator
+// sums into acc[2*solves], 2 adjoint without sums.
+cudaError_t launch_colpass(int n, int mode, float2 *A, float2 *F, const InstDesc *d, double *acc, cudaStream_t st,
+                           int solves = 1);
 cudaError_t launch_abs2_sum(const float2 *S, int nn, double *out, cudaStream_t st);
 cudaError_t launch_seed_cotangent(const float2 *S, float2 *cP, float2 *cS, int nn, const double *g, cudaStream_t st);
 

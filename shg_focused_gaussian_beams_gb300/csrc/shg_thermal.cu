@@ -332,55 +332,6 @@ __global__ void k_sellmeier_tables(const float *__restrict__ T, float *NP, float
 // The coupling per pixel follows Solver.h:44-63: n from T(x,y,slice), phase
 // DKint*(dz*inc + (s+1)*dz)/(s+1) with inc = 0, 0.25, 0.25, 0.5 for the four stages.
 
-struct ThCoef {
-    float4 c0, c1, c2;  // stage constants for inc = 0, 0.25 (stages 2, 3), 0.5 (stage 4)
-    float tpa1;
-};
-
-__device__ __forceinline__ ThCoef th_coef(const ThermDesc &t, float np, float ns, float dkint, int s, float dz) {
-    ThCoef r;
-    const float kp = t.pidq / (np * t.lp);
-    const float ks = t.hpidq / (ns * t.ls);
-    const float sp1 = (float)(s + 1);
-    const float base = sp1 * dz;
-    const float ph0 = (dkint * base) / sp1;
-    const float ph1 = (dkint * (dz * 0.25f + base)) / sp1;
-    const float ph2 = (dkint * (dz * 0.5f + base)) / sp1;
-    float sn, cs;
-    sincosf(ph0, &sn, &cs);
-    r.c0 = make_float4(kp * sn, kp * cs, -ks * sn, ks * cs);
-    sincosf(ph1, &sn, &cs);
-    r.c1 = make_float4(kp * sn, kp * cs, -ks * sn, ks * cs);
-    sincosf(ph2, &sn, &cs);
-    r.c2 = make_float4(kp * sn, kp * cs, -ks * sn, ks * cs);
-    r.tpa1 = t.tpa_c * ns;
-    return r;
-}
-
-__device__ __forceinline__ void rk4_point_th(float2 &P, float2 &S, const ThCoef &k, const InstDesc &d) {
-    float2 kp, ks, ap, as, accp, accs;
-    dadz_point(P, S, k.c0, d.hp, d.tpa0, k.tpa1, kp, ks);
-    accp = kp;
-    accs = ks;
-    ap = make_float2(fmaf(0.5f, kp.x, P.x), fmaf(0.5f, kp.y, P.y));
-    as = make_float2(fmaf(0.5f, ks.x, S.x), fmaf(0.5f, ks.y, S.y));
-    dadz_point(ap, as, k.c1, d.hp, d.tpa0, k.tpa1, kp, ks);
-    accp = make_float2(fmaf(2.0f, kp.x, accp.x), fmaf(2.0f, kp.y, accp.y));
-    accs = make_float2(fmaf(2.0f, ks.x, accs.x), fmaf(2.0f, ks.y, accs.y));
-    ap = make_float2(fmaf(0.5f, kp.x, P.x), fmaf(0.5f, kp.y, P.y));
-    as = make_float2(fmaf(0.5f, ks.x, S.x), fmaf(0.5f, ks.y, S.y));
-    dadz_point(ap, as, k.c1, d.hp, d.tpa0, k.tpa1, kp, ks);
-    accp = make_float2(fmaf(2.0f, kp.x, accp.x), fmaf(2.0f, kp.y, accp.y));
-    accs = make_float2(fmaf(2.0f, ks.x, accs.x), fmaf(2.0f, ks.y, accs.y));
-    ap = c_add(P, kp);
-    as = c_add(S, ks);
-    dadz_point(ap, as, k.c2, d.hp, d.tpa0, k.tpa1, kp, ks);
-    accp = c_add(accp, kp);
-    accs = c_add(accs, ks);
-    P = make_float2(fmaf(accp.x, d.dz6, P.x), fmaf(accp.y, d.dz6, P.y));
-    S = make_float2(fmaf(accs.x, d.dz6, S.x), fmaf(accs.y, d.dz6, S.y));
-}
-
 __device__ __forceinline__ void block_add_double_th(double v, double *dst) {
     __shared__ double red[32];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

@@ -188,8 +188,7 @@ int ThermalSolve::jacobi(float t_inf, int *counter) {
     return SHG_OK;
 }
 
-int ThermalSolve::cwes(float power, float waist, float focal) {
-    const size_t nn = (size_t)n_ * n_;
+int ThermalSolve::tables() {
     const float PI = (float)3.14159265358979323846;
     const float lp = cfg_.lp, ls = (float)(0.5 * (double)lp);
     // PhaseMatching.h:105 -> 41: delta-k and the indices from T.
@@ -198,19 +197,6 @@ int ThermalSolve::cwes(float power, float waist, float focal) {
     const size_t ic = (size_t)(n_ / 2) * n_ + (size_t)(n_ / 2);
     TH_CUDA(cudaMemcpyAsync(&tc_, T_cur() + ic, sizeof(float), cudaMemcpyDeviceToHost, st_));
     TH_CUDA(cudaStreamSynchronize(st_));
-    SolveParams sp{n_, nz_, cfg_.lx, cfg_.ly, power, waist, focal, tc_, tc_, tc_};
-    std::memset(&h_desc_, 0, sizeof(h_desc_));
-    fill_scalars(cfg_, sp, h_desc_);
-    h_desc_.P = f_;
-    h_desc_.S = f_ + nn;
-    h_desc_.Pout = f_ + 2 * nn;
-    h_desc_.Sout = f_ + 3 * nn;
-    h_desc_.Hp = f_ + 4 * nn;
-    h_desc_.Hs = f_ + 5 * nn;
-    h_desc_.stepc = stepc_;
-    h_desc_.acc = acc_;
-    h_desc_.nsteps = nz_;
-    h_desc_.pump_given = 0;
     const float dQ = (float)((2.0 / (double)PI) * (double)cfg_.deff);
     const float C = (float)(299792458 * 1E6 / 1E12), EPS0 = (float)(8.8541878128E-12 * 1E12 / 1E6);
     th_.nx = n_;
@@ -231,6 +217,31 @@ int ThermalSolve::cwes(float power, float waist, float focal) {
     th_.beta_s = cfg_.beta_s;
     th_.kth = cfg_.kth;
     th_.tpa_c = (float)(0.25 * (double)cfg_.beta_s * (double)EPS0 * (double)C);
+    return SHG_OK;
+}
+
+int ThermalSolve::load_temperature(const float *T_host) {
+    TH_CUDA(cudaMemcpyAsync(T_cur(), T_host, tsize_ * sizeof(float), cudaMemcpyHostToDevice, st_));
+    TH_TRY(tables());
+    return SHG_OK;
+}
+
+int ThermalSolve::cwes(float power, float waist, float focal) {
+    const size_t nn = (size_t)n_ * n_;
+    TH_TRY(tables());
+    SolveParams sp{n_, nz_, cfg_.lx, cfg_.ly, power, waist, focal, tc_, tc_, tc_};
+    std::memset(&h_desc_, 0, sizeof(h_desc_));
+    fill_scalars(cfg_, sp, h_desc_);
+    h_desc_.P = f_;
+    h_desc_.S = f_ + nn;
+    h_desc_.Pout = f_ + 2 * nn;
+    h_desc_.Sout = f_ + 3 * nn;
+    h_desc_.Hp = f_ + 4 * nn;
+    h_desc_.Hs = f_ + 5 * nn;
+    h_desc_.stepc = stepc_;
+    h_desc_.acc = acc_;
+    h_desc_.nsteps = nz_;
+    h_desc_.pump_given = 0;
     TH_CUDA(cudaMemcpyAsync(d_desc_, &h_desc_, sizeof(InstDesc), cudaMemcpyHostToDevice, st_));
     TH_CUDA(cudaMemsetAsync(acc_, 0, 4 * sizeof(double), st_));
     TH_CUDA(cudaMemsetAsync(acc_ + 4, 0, sizeof(double), st_));  // solve index 0 for the column pass

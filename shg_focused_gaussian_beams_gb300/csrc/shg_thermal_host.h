@@ -40,6 +40,17 @@ class ThermalSolve {
     int sweeps(float t_inf, int n);          // n plain sweeps
     int cwes(float power, float waist, float focal);  // one thermal CWES from the current T
 
+    // Indices and delta-k of the current T (PhaseMatching.h:41-54), the centre temperature
+    // and the coupling constants; run by cwes() first.
+    int tables();
+    // Replaces the current temperature field (host, NX*NY*NZ) and builds its tables.
+    int load_temperature(const float *T_host);
+    const float *NP() const { return np_; }
+    const float *NS() const { return ns_; }
+    const float *DK() const { return dk_; }
+    const ThermDesc &therm() const { return th_; }
+    float center_temperature() const { return tc_; }
+
     float *T_cur() { return T_[cur_]; }
     float *T_prev() { return T_[cur_ ^ 1]; }
     float *QK() { return qk_; }

@@ -247,6 +247,110 @@ class Sweep:
         return v.value
 
 
+class ThermalGradBatch:
+    """Batched gradient of the THERMAL z-march with each solve's temperature field held
+    fixed (``shg_thgrad_*``). Solve i's temperature comes from Solver::run (THERMAL) with a
+    Gaussian pump (``solve_temperature``) or is given (``set_temperature``); its loss is the
+    SH output power, differentiated with respect to its input pump. Pumps are torch
+    complex64 CUDA tensors of shape (count, NY, NX)."""
+
+    def __init__(self, count, crystal=None, nx=64, ny=64, nz=200, lx=None, ly=None, bc=0, device=0):
+        kw = dict(nx=nx, ny=ny, nz=nz, thermal=1, bc=bc, device=device)
+        if lx is not None:
+            kw["lx"] = float(lx)
+        if ly is not None:
+            kw["ly"] = float(ly)
+        self.cfg = _cfg_from(crystal, **kw)
+        h = C.c_void_p()
+        check(lib().shg_thgrad_create(C.byref(self.cfg), int(count), C.byref(h)), "shg_thgrad_create")
+        self._h = h
+        self.count, self.nx, self.ny, self.nz = int(count), nx, ny, nz
+        self.device = device
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().shg_thgrad_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def solve_temperature(self, i, power, waist, focal, temp, t_inf=25.0, t_peltier1=None, t_peltier2=None):
+        """Solver::run (THERMAL, Solver.h:287-340) for solve i; returns its Jacobi counts."""
+        t1 = temp if t_peltier1 is None else t_peltier1
+        t2 = t1 if t_peltier2 is None else t_peltier2
+        c = (C.c_int * 5)()
+        check(lib().shg_thgrad_solve_temperature(self._h, int(i), power, waist, focal, temp, t_inf, t1, t2, c),
+              "shg_thgrad_solve_temperature")
+        return list(c)
+
+    def set_temperature(self, i, T: np.ndarray, power, waist, focal):
+        Tn = np.ascontiguousarray(T, np.float32)
+        assert Tn.size == self.nx * self.ny * self.nz
+        check(lib().shg_thgrad_set_temperature(self._h, int(i), _pf(Tn), power, waist, focal),
+              "shg_thgrad_set_temperature")
+
+    def temperature(self, i):
+        T = np.zeros((self.nz, self.ny, self.nx), np.float32)
+        check(lib().shg_thgrad_get_temperature(self._h, int(i), _pf(T)), "shg_thgrad_get_temperature")
+        return T
+
+    def _stream(self, t, stream):
+        import torch
+        return torch.cuda.current_stream(t.device).cuda_stream if stream is None else stream
+
+    def gaussian_pumps(self, stream=None):
+        import torch
+        out = torch.empty((self.count, self.ny, self.nx), dtype=torch.complex64, device=f"cuda:{self.device}")
+        check(lib().shg_thgrad_gaussian_pumps(self._h, out.data_ptr(), self._stream(out, stream)),
+              "shg_thgrad_gaussian_pumps")
+        return out
+
+    def _check_pump(self, pump):
+        import torch
+        assert pump.dtype == torch.complex64 and pump.is_cuda and pump.is_contiguous()
+        assert tuple(pump.shape) == (self.count, self.ny, self.nx)
+
+    def forward(self, pump, with_fields=False, stream=None):
+        """Returns dict(p_sh, p_in [W] as numpy arrays, and with_fields: pump_out, sh_out)."""
+        import torch
+        self._check_pump(pump)
+        po = torch.empty_like(pump) if with_fields else None
+        so = torch.empty_like(pump) if with_fields else None
+        psh = np.zeros(self.count)
+        pin = np.zeros(self.count)
+        check(lib().shg_thgrad_forward(self._h, pump.data_ptr(), None if po is None else po.data_ptr(),
+                                       None if so is None else so.data_ptr(), psh.ctypes.data_as(C.POINTER(C.c_double)),
+                                       pin.ctypes.data_as(C.POINTER(C.c_double)), self._stream(pump, stream)),
+              "shg_thgrad_forward")
+        r = {"p_sh": psh, "p_in": pin}
+        if with_fields:
+            r.update(pump_out=po, sh_out=so)
+        return r
+
+    def gradient(self, pump, checkpoints=20, grad=None, stream=None):
+        """Returns dict(p_sh, p_in, grad) with grad[i] = dP_SH,i / dA_in,i (dL/dRe + i dL/dIm)."""
+        import torch
+        self._check_pump(pump)
+        g = torch.empty_like(pump) if grad is None else grad
+        psh = np.zeros(self.count)
+        pin = np.zeros(self.count)
+        check(lib().shg_thgrad_gradient(self._h, pump.data_ptr(), int(checkpoints), g.data_ptr(),
+                                        psh.ctypes.data_as(C.POINTER(C.c_double)),
+                                        pin.ctypes.data_as(C.POINTER(C.c_double)), self._stream(pump, stream)),
+              "shg_thgrad_gradient")
+        return {"p_sh": psh, "p_in": pin, "grad": g}
+
+    def launch_count(self) -> int:
+        return int(lib().shg_thgrad_launch_count(self._h))
+
+    def device_bytes(self) -> float:
+        return float(lib().shg_thgrad_device_bytes(self._h))
+
+
 def _grid_cfg(crystal, nx, ny, nz, lx=None, ly=None):
     kw = dict(nx=nx, ny=ny, nz=nz)
     if lx is not None:

@@ -1,6 +1,7 @@
 """Shared helpers for the tests (not collected)."""
 from __future__ import annotations
 
+import math
 import os
 
 import numpy as np
@@ -47,3 +48,12 @@ def bits_equal(a, b):
     a = np.ascontiguousarray(a)
     b = np.ascontiguousarray(b)
     return a.shape == b.shape and a.tobytes() == b.tobytes()
+
+
+def smooth_noise(rng, n, cells=8):
+    """Seeded complex Gaussian field smoothed over `cells` grid cells (FFT low-pass)."""
+    a = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    k = np.fft.fftfreq(n)
+    g = np.exp(-0.5 * (k[:, None] ** 2 + k[None, :] ** 2) * (2 * math.pi * cells / 2.355) ** 2)
+    b = np.fft.ifft2(np.fft.fft2(a) * g)
+    return b / np.sqrt(np.mean(np.abs(b) ** 2))

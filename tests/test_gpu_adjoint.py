@@ -13,6 +13,7 @@ import numpy as np
 import pytest
 
 import oracle as O
+from _util import smooth_noise
 
 pytestmark = pytest.mark.gpu
 
@@ -26,15 +27,6 @@ from shg_focused_gaussian_beams_gb300.solver import Solver  # noqa: E402
 
 FD_RTOL = 1e-3
 N, NZ, T0, P0 = 64, 40, 50.0, 20.0
-
-
-def smooth_noise(rng, n, cells=8):
-    """Seeded complex Gaussian field smoothed over `cells` grid cells (FFT low-pass)."""
-    a = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
-    k = np.fft.fftfreq(n)
-    g = np.exp(-0.5 * (k[:, None] ** 2 + k[None, :] ** 2) * (2 * math.pi * cells / 2.355) ** 2)
-    b = np.fft.ifft2(np.fft.fft2(a) * g)
-    return b / np.sqrt(np.mean(np.abs(b) ** 2))
 
 
 @pytest.fixture(scope="module")

@@ -59,6 +59,24 @@ def test_thermal_golden_bitexact(name):
     assert bits_equal(res["pump"], g["pump_out"])
 
 
+@pytest.mark.parametrize("name", ["thermal_topopen.npz", "thermal_oven.npz"])
+def test_fixed_temperature_cwes_reproduces_the_last_outer_iteration(name):
+    """The THERMAL CWES with T held fixed (the gradient workload's forward map): from the
+    reference run's final temperature field and the Gaussian pump at T[NX/2, NY/2, 0] it
+    reproduces the reference's output fields bit for bit (the last outer iteration ran on
+    that field); the double-precision version with the float delta-k table agrees to
+    float rounding."""
+    g = golden(name)
+    o = O.Oracle(cfg_from_golden(g))
+    T = g["T"]
+    tc = float(T[0, T.shape[1] // 2, T.shape[2] // 2])
+    pump = o.set_pump(float(g["power"]), float(np.float32(0.5 * 30000.0)), float(g["waist"]), tc)
+    po, so = o.cwes_thermal(T, pump, np.zeros_like(pump), tc)
+    assert bits_equal(so, g["sh_out"]) and bits_equal(po, g["pump_out"])
+    po64, so64 = o.cwes_thermal64(T, pump, np.zeros_like(pump), tc, dk3=o.dk_thermal(T))
+    assert rel_l2(so64, g["sh_out"]) < FIELD_RTOL and rel_l2(po64, g["pump_out"]) < FIELD_RTOL
+
+
 @pytest.mark.parametrize("n0,n1", [(64, 64), (128, 128), (32, 16), (48, 48), (12, 20)])
 @pytest.mark.parametrize("sign", [-1, 1])
 def test_dft_restatement_vs_numpy(n0, n1, sign):
