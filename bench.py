@@ -139,6 +139,70 @@ def run_adjoint(args):
                       "store_all_dT_rel_diff": abs(r_all["dT"] - r["dT"]) / abs(r["dT"])}), flush=True)
 
 
+def run_thermal_adjoint(args, count=64, n=256, nz=400, design_steps=20):
+    """Batched adjoint with THERMAL: 64 solves of 256x256x400 (P ~ U(5, 40) W, xi = 2.84,
+    oven 50 C + U(-1, 1) K), Hermite-Gauss (m, n <= 3) admixtures |c| <= 0.2 on a Gaussian;
+    each temperature field is solved once (Solver::run, THERMAL) and held fixed. Times the
+    batched forward and gradient passes (CUDA events) and the 20-step design loop."""
+    import torch
+    from shg_focused_gaussian_beams_gb300 import inverse as I
+    from shg_focused_gaussian_beams_gb300.solver import ThermalGradBatch
+    insts = W.config_thermal_adjoint(count, n=n, nz=nz)
+    i0 = insts[0]
+    focal = float(np.float32(0.5 * W.CRYSTAL_QPM50.lz))
+    tb = ThermalGradBatch(count, crystal=W.CRYSTAL_QPM50, nx=n, ny=n, nz=nz, lx=i0.lx, ly=i0.ly, bc=1)
+    t0 = time.time()
+    counts = [tb.solve_temperature(i, x.power, x.waist, focal, x.temp, 25.0, x.t1, x.t2) for i, x in enumerate(insts)]
+    t_temp = time.time() - t0
+    tcs = [float(tb.temperature(i)[0, n // 2, n // 2]) for i in range(count)]
+    modes = torch.stack([I.hermite_gauss_modes(n, n, i0.lx, i0.ly, x.waist, focal, tc, mmax=3)[0]
+                         for x, tc in zip(insts, tcs)])
+    coef0 = I.seeded_admixtures(count, modes.shape[1], seed=77, cmax=0.2)
+    power = torch.tensor([x.power for x in insts], dtype=torch.float64, device="cuda")
+    pumps = I.pumps_from_coefficients(coef0.cuda(), modes, power).to(torch.complex64).contiguous()
+    st = torch.cuda.current_stream()
+    for _ in range(max(args.warmup, 1)):
+        tb.forward(pumps)
+        tb.gradient(pumps, checkpoints=20)
+    torch.cuda.synchronize()
+
+    def timed(fn, reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            fn()
+        e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+    reps = max(args.steps, 1)
+    fwd = timed(lambda: tb.forward(pumps), reps)
+    n_fwd = tb.launch_count()
+    grd = timed(lambda: tb.gradient(pumps, checkpoints=20), reps)
+    n_grd = tb.launch_count()
+    mem20 = tb.device_bytes()
+    tb.gradient(pumps, checkpoints=nz - 1)
+    grd_all = timed(lambda: tb.gradient(pumps, checkpoints=nz - 1), reps)
+    mem_all = tb.device_bytes()
+    t0 = time.time()
+    _, hist = I.optimize_inputs(tb, coef0, modes, power, steps=design_steps, lr=0.05, checkpoints=nz - 1)
+    torch.cuda.synchronize()
+    t_design = time.time() - t0
+    units = count * n * n * (nz - 1)
+    print(json.dumps({
+        "workload": f"thermal_adjoint: {count} solves {n}x{n}x{nz}, P~U(5,40) W, xi=2.84, oven 50+U(-1,1) C, "
+                    "HG(m,n<=3) admixtures |c|<=0.2, T solved once then fixed",
+        "temperature_solves_s": t_temp, "jacobi_counts_first": counts[0],
+        "forward_ms": fwd, "forward_launches": n_fwd,
+        "forward_grid_pt_steps_per_s": units / (fwd * 1e-3),
+        "gradient_ms_20_checkpoints": grd, "gradient_launches": n_grd, "gradient_over_forward": grd / fwd,
+        "gradient_ms_store_all": grd_all, "store_all_over_forward": grd_all / fwd,
+        "device_gb_20_checkpoints": mem20 / 1e9, "device_gb_store_all": mem_all / 1e9,
+        "design_loop_s": t_design, "design_steps": design_steps,
+        "eta_mean_before": float(hist[0].mean()), "eta_mean_after": float(hist[-1].mean()),
+        "eta_improved_solves": int((hist[-1] > hist[0]).sum()),
+    }), flush=True)
+
+
 def run_heat(args):
     """Heat sweeps alone on the 256x256x400 THERMAL grid (profiling case)."""
     inst = W.config_thermal_256()
@@ -428,7 +492,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["sweep", "plain128", "rows256", "thermal256", "heat256", "adjoint256"], default="sweep")
+    ap.add_argument("--workload", choices=["sweep", "plain128", "rows256", "thermal256", "heat256", "adjoint256", "thermal_adjoint"],
+                    default="sweep")
     args = ap.parse_args()
     if args.workload == "thermal256":
         run_thermal(args)
@@ -436,6 +501,8 @@ def main():
         run_heat(args)
     elif args.workload == "adjoint256":
         run_adjoint(args)
+    elif args.workload == "thermal_adjoint":
+        run_thermal_adjoint(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

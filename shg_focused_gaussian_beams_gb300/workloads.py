@@ -130,6 +130,22 @@ def config_thermal_256(seed: int = 1234, n: int = 256, nz: int = 400) -> Instanc
                     t1=t_oven, t2=t_oven, thermal=True, bc=1)
 
 
+def config_thermal_adjoint(count: int = 64, seed: int = 4242, n: int = 256, nz: int = 400) -> list[Instance]:
+    """Batched THERMAL gradient workload: `count` solves of n x n x nz, pump power U(5, 40) W,
+    xi = 2.84 (waist at 50 C), window 16 w0, oven-surrounded faces at 50 C + U(-1, 1) K;
+    each solve's temperature field is solved once and then held fixed."""
+    rng = random.Random(seed)
+    w0 = waist_for_xi(2.84, PM_TEMP_C)
+    win = float(F32(16.0 * w0))
+    out = []
+    for _ in range(count):
+        p = float(F32(rng.uniform(5.0, 40.0)))
+        t = float(F32(PM_TEMP_C + rng.uniform(-1.0, 1.0)))
+        out.append(Instance(nx=n, ny=n, nz=nz, lx=win, ly=win, power=p, waist=w0, temp=t, t1=t, t2=t,
+                            thermal=True, bc=1))
+    return out
+
+
 def config_sweep(count: int = 512, seed: int = 2024) -> list[Instance]:
     """Batched sweep: per instance P log-U(1, 50) W, xi U(0.5, 5), T = 50 C + U(-2, 2) K,
     N in {64, 128, 256}, Nz in {100, 200, 400}; window 16 w0."""
