@@ -400,6 +400,24 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def per_instance_rate(sample, device):
+    """Solves one at a time through the single-solve API (shg_run: graph launch, sync)."""
+    from shg_focused_gaussian_beams_gb300.solver import Solver
+    hs = [Solver(crystal=W.CRYSTAL_QPM50, nx=i.nx, ny=i.ny, nz=i.nz, lx=i.lx, ly=i.ly, device=device)
+          for i in sample]
+    for h, i in zip(hs, sample):
+        h.run(i.power, i.waist, i.focal, i.temp)
+    t0 = time.perf_counter()
+    for h, i in zip(hs, sample):
+        h.run(i.power, i.waist, i.focal, i.temp)
+    dt = time.perf_counter() - t0
+    for h in hs:
+        h.close()
+    return {"solves_per_s": len(sample) / dt, "pt_steps_per_s": pt_steps(sample) / dt, "sample_solves": len(sample),
+            "note": "the first 64 solves of the same workload, one Solver::run each (single-solve graph, "
+                    "synchronised), handles created and warmed outside the timed region"}
+
+
 def run_ours(args):
     import torch
     from shg_focused_gaussian_beams_gb300.solver import Sweep
@@ -449,6 +467,10 @@ def run_ours(args):
            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": len(insts) * 8 + d2h_fields,
            "solves_per_s": len(insts) * world * args.steps / e2e_s}
 
+    # the plain per-instance GPU path on a sample of the same solves: one solve at a time
+    # through Solver::run (handles created and warmed outside the timed region)
+    per = per_instance_rate(insts[:64], local) if rank == 0 else None
+
     # roofline of the dominant kernel from an instrumented run (per-launch CUDA events)
     prof = sw.profile()
     dom = max(prof, key=lambda k: prof[k][1])
@@ -479,7 +501,11 @@ def run_ours(args):
                 "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": cores, "kind": "port",
                                  "sample": f"{len(sample)} solves of the workload (N<=128, Nz<=200) on {cores} "
                                            f"threads, median of {len(cpu_times)} runs; oracle restatement, FP32"},
-                "eta_mean": float(np.mean(eta))}
+                "eta_mean": float(np.mean(eta)),
+                "per_instance_gpu": per,
+                "batched_over_per_instance": {"solves_per_s": solves_s / world / per["solves_per_s"],
+                                              "pt_steps_per_s": value / world / per["pt_steps_per_s"]},
+                "schedule": sw.schedule()}
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist

@@ -154,6 +154,21 @@ int shg_batch_io_bytes(shg_batch *b, long long *h2d_per_run, long long *d2h_fiel
 /* Number of kernel launches one run issues. */
 int shg_batch_launch_count(shg_batch *b, int *launches);
 
+/* Schedule autotuner. Each grid-size class of the batch marches either as streaming
+ * row/column launches or as one persistent resident launch (a thread-block cluster per
+ * solve, fields in shared memory) in one of several (cluster size, CTAs per SM) variants.
+ * Unless the environment variable SHG_MARCH is "streaming" or "resident", the first run
+ * times every candidate on the class's own solves and keeps the fastest (cached per
+ * device and class shape for the process). shg_batch_autotune does that now, outside any
+ * stream capture; shg_batch_schedule writes the choices and trial times as text. */
+int shg_batch_autotune(shg_batch *b, void *stream);
+/* Fixes the schedule of the class with grid n: resident = 0 streaming, else the resident
+ * variant with cluster_size CTAs per cluster and ctas_per_sm CTAs per SM (variants: n <= 32
+ * (1, 1); n = 64 (1, 1), (1, 2), (2, 2), (2, 4); n = 128 (2, 1), (4, 1), (4, 2); n = 256
+ * (8, 1), (16, 1), (16, 2)). SHG_ERR_UNSUPPORTED if the variant does not exist or fit. */
+int shg_batch_set_schedule(shg_batch *b, int n, int resident, int cluster_size, int ctas_per_sm);
+int shg_batch_schedule(shg_batch *b, char *buf, int len);
+
 /* Per-kernel timing of one un-captured run: CUDA events around every launch, summed per
  * kernel (name like "rows<128>"), with the algorithmic bytes those launches must move
  * (fields read and written once; propagators read once in the column pass). */

@@ -11,6 +11,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <tuple>
 #include <random>
 #include <string>
 #include <vector>
@@ -145,7 +146,8 @@ int ensure_twiddles(int device) {
             tab[N + m] = make_float2((float)std::cos(a), (float)(-std::sin(a)));
         }
     for (const float2 *addr : {twiddle_symbol_address_march(), twiddle_symbol_address_thermal(),
-                               twiddle_symbol_address_adjoint(), twiddle_symbol_address_resident()}) {
+                               twiddle_symbol_address_adjoint(), twiddle_symbol_address_resident(),
+                               twiddle_symbol_address_resident128(), twiddle_symbol_address_resident256()}) {
         void *p = const_cast<float2 *>(addr);
         if (!p) {
             set_error("twiddle table symbol unavailable");
@@ -250,10 +252,18 @@ class Batch {
             }
             classes_.push_back(c);
         }
-        resident_ = !(std::getenv("SHG_MARCH") && std::string(std::getenv("SHG_MARCH")) == "streaming");
+        // schedule per class: SHG_MARCH=streaming | resident (default variant) | auto (default:
+        // the autotuner picks at the first run)
+        const char *mode = std::getenv("SHG_MARCH");
+        const std::string m = mode ? mode : "auto";
         for (auto &c : classes_) {
             for (int k = 0; k < c.count; ++k) c.pt_steps += (double)c.n * c.n * c.steps[k];
-            if (resident_) SHG_CUDA(prepare_resident(c.n, &c.max_clusters));
+            c.tuned = m != "auto";
+            c.resident = m != "streaming";
+            if (c.resident) {
+                c.var = resident_default(c.n);
+                SHG_CUDA(prepare_resident(c.n, c.var, &c.max_clusters));
+            }
         }
         // resident march: class streams (largest solves first) and one job counter per class
         while ((int)side_streams_.size() < (int)classes_.size()) {
@@ -334,6 +344,7 @@ class Batch {
     // Enqueue set-up and the march for every solve on `st` (a CUDA graph after the
     // first call when use_graph is set).
     int run_async(cudaStream_t st, bool use_graph) {
+        SHG_TRY_INT(tune(st));
         if (desc_dirty_) {
             SHG_CUDA(cudaMemcpyAsync(d_desc_, desc_.data(), desc_.size() * sizeof(InstDesc), cudaMemcpyHostToDevice, st));
             desc_dirty_ = false;
@@ -362,12 +373,163 @@ class Batch {
 
     int launch_count() const {
         int c = 2;  // set-up kernels
-        if (resident_) return c + (int)classes_.size();
         for (const auto &k : classes_) {
             const int K = k.steps.empty() ? 0 : k.steps[0];
-            c += (K + 1) + K;
+            c += k.resident ? 1 : (K + 1) + K;
         }
         return c;
+    }
+
+    // Autotuner: for every class not yet scheduled, time the streaming schedule and each
+    // resident variant on the class's own solves (set-up included in every trial, the
+    // second of two runs counted) and keep the fastest. Choices are cached per device and
+    // class shape (grid, solve count, step total) for the life of the process.
+    int tune(cudaStream_t st) {
+        bool any = false;
+        for (auto &c : classes_) any |= !c.tuned;
+        if (!any) return SHG_OK;
+        if (desc_dirty_) {
+            SHG_CUDA(cudaMemcpyAsync(d_desc_, desc_.data(), desc_.size() * sizeof(InstDesc), cudaMemcpyHostToDevice, st));
+            desc_dirty_ = false;
+        }
+        static std::mutex mu;
+        static std::map<std::tuple<int, int, int, double>, std::pair<bool, ResidentVariant>> cache;
+        cudaEvent_t a, b;
+        SHG_CUDA(cudaEventCreate(&a));
+        SHG_CUDA(cudaEventCreate(&b));
+        int rc = SHG_OK;
+        for (int ci = 0; ci < (int)classes_.size() && rc == SHG_OK; ++ci) {
+            Class &c = classes_[ci];
+            if (c.tuned) continue;
+            const auto key = std::make_tuple(cr_.device, c.n, c.count, c.pt_steps);
+            {
+                std::lock_guard<std::mutex> lock(mu);
+                auto it = cache.find(key);
+                if (it != cache.end()) {
+                    c.resident = it->second.first;
+                    c.var = it->second.second;
+                    if (c.resident) rc = prepare_resident(c.n, c.var, &c.max_clusters) == cudaSuccess ? SHG_OK : SHG_ERR_CUDA;
+                    c.tuned = true;
+                    continue;
+                }
+            }
+            struct Cand {
+                bool resident;
+                ResidentVariant v;
+                int clusters;
+            };
+            std::vector<Cand> cands{{false, {0, 0}, 0}};
+            ResidentVariant vs[8];
+            const int nv = resident_variants(c.n, vs, 8);
+            for (int i = 0; i < nv; ++i) {
+                int mc = 0;
+                if (prepare_resident(c.n, vs[i], &mc) == cudaSuccess && mc > 0)
+                    cands.push_back({true, vs[i], mc});
+                else
+                    cudaGetLastError();  // a variant that does not fit is skipped
+            }
+            float best = 1e30f;
+            int bi = 0;
+            c.trials.clear();
+            for (int i = 0; i < (int)cands.size() && rc == SHG_OK; ++i) {
+                c.resident = cands[i].resident;
+                c.var = cands[i].v;
+                c.max_clusters = cands[i].clusters;
+                float ms = 0.f;
+                for (int rep = 0; rep < 2 && rc == SHG_OK; ++rep) {
+                    rc = enqueue_inputs(st);
+                    if (rc) break;
+                    if (launch_setup(d_desc_, (int)desc_.size(), max_nn_, max_nz_, st) != cudaSuccess ||
+                        cudaMemsetAsync(d_counters_, 0, 64 * sizeof(int), st) != cudaSuccess ||
+                        cudaEventRecord(a, st) != cudaSuccess) {
+                        rc = SHG_ERR_CUDA;
+                        break;
+                    }
+                    rc = enqueue_class(ci, st, nullptr);
+                    if (rc) break;
+                    if (cudaEventRecord(b, st) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess ||
+                        cudaEventElapsedTime(&ms, a, b) != cudaSuccess)
+                        rc = SHG_ERR_CUDA;
+                }
+                c.trials.push_back({cands[i].resident, cands[i].v, ms});
+                if (ms < best) {
+                    best = ms;
+                    bi = i;
+                }
+            }
+            if (rc) break;
+            c.resident = cands[bi].resident;
+            c.var = cands[bi].v;
+            c.max_clusters = cands[bi].clusters;
+            c.tuned = true;
+            std::lock_guard<std::mutex> lock(mu);
+            cache[key] = {c.resident, c.var};
+        }
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        if (rc && rc != SHG_ERR_CUDA) return rc;
+        if (rc) {
+            set_error("autotune: CUDA error while timing a schedule");
+            return rc;
+        }
+        invalidate_graph();
+        return SHG_OK;
+    }
+
+    // Fixes the schedule of grid-size class n: streaming (resident = 0) or the resident
+    // variant (cs, minb), which must be one of resident_variants(n) and fit on the device.
+    int set_schedule(int n, int resident, int cs, int minb) {
+        for (auto &c : classes_) {
+            if (c.n != n) continue;
+            if (!resident) {
+                c.resident = false;
+            } else {
+                ResidentVariant vs[8];
+                const int nv = resident_variants(n, vs, 8);
+                bool ok = false;
+                for (int i = 0; i < nv; ++i) ok |= vs[i].cs == cs && vs[i].minb == minb;
+                int mc = 0;
+                if (!ok || prepare_resident(n, ResidentVariant{cs, minb}, &mc) != cudaSuccess || mc < 1) {
+                    cudaGetLastError();
+                    set_error("set_schedule: no such resident variant for this grid, or it does not fit");
+                    return SHG_ERR_UNSUPPORTED;
+                }
+                c.resident = true;
+                c.var = ResidentVariant{cs, minb};
+                c.max_clusters = mc;
+            }
+            c.tuned = true;
+            invalidate_graph();
+            return SHG_OK;
+        }
+        set_error("set_schedule: no class with that grid size");
+        return SHG_ERR_INVALID;
+    }
+
+    // One line per class: grid, solves, chosen schedule and the trial times (ms).
+    std::string schedule() const {
+        std::string out;
+        for (const auto &c : classes_) {
+            out += "n=" + std::to_string(c.n) + " solves=" + std::to_string(c.count) + ": ";
+            out += !c.tuned ? "untuned" : c.resident ? "resident cs=" + std::to_string(c.var.cs) +
+                                                             " minb=" + std::to_string(c.var.minb)
+                                                       : std::string("streaming");
+            if (!c.trials.empty()) {
+                out += " [";
+                for (size_t i = 0; i < c.trials.size(); ++i) {
+                    const auto &t = c.trials[i];
+                    char buf[96];
+                    std::snprintf(buf, sizeof(buf), "%s%s %.3f", i ? ", " : "",
+                                  t.resident ? ("cs" + std::to_string(t.v.cs) + "/" + std::to_string(t.v.minb)).c_str()
+                                             : "streaming",
+                                  t.ms);
+                    out += buf;
+                }
+                out += " ms]";
+            }
+            out += "\n";
+        }
+        return out;
     }
 
     int copy_acc(std::vector<double> &acc) {
@@ -405,11 +567,20 @@ class Batch {
     const SolveParams &params(int i) const { return sp_[i]; }
 
    private:
+    struct Trial {
+        bool resident;
+        ResidentVariant v;
+        float ms;
+    };
     struct Class {
         int n = 0, offset = 0, count = 0;
         std::vector<int> steps;  // descending
+        bool tuned = false;      // schedule chosen (by SHG_MARCH or the autotuner)
+        bool resident = true;    // resident march (else streaming row / column launches)
+        ResidentVariant var{1, 1};
         int max_clusters = 0;    // resident march: clusters resident at once
         double pt_steps = 0;     // sum of n*n*nsteps
+        std::vector<Trial> trials;
     };
 
    public:
@@ -442,6 +613,7 @@ class Batch {
     };
 
     int profile(cudaStream_t st, Recorder &rec) {
+        SHG_TRY_INT(tune(st));
         if (desc_dirty_) {
             SHG_CUDA(cudaMemcpyAsync(d_desc_, desc_.data(), desc_.size() * sizeof(InstDesc), cudaMemcpyHostToDevice, st));
             desc_dirty_ = false;
@@ -499,50 +671,52 @@ class Batch {
                 SHG_CUDA(cudaMemcpyAsync(desc_[i].slices + nn, desc_[i].S, nn * sizeof(float2),
                                          cudaMemcpyDeviceToDevice, st));
             }
-        if (resident_) {
-            SHG_CUDA(cudaMemsetAsync(d_counters_, 0, 64 * sizeof(int), st));
-            // classes in descending grid size; concurrently on side streams unless timed
-            std::vector<int> order(classes_.size());
-            for (int i = 0; i < (int)order.size(); ++i) order[i] = i;
-            std::sort(order.begin(), order.end(), [&](int a, int b) { return classes_[a].n > classes_[b].n; });
-            if (!rec) SHG_CUDA(cudaEventRecord(fork_event_, st));
-            for (int oi = 0; oi < (int)order.size(); ++oi) {
-                const Class &k = classes_[order[oi]];
-                const int *list = d_lists_ + k.offset;
-                int *counter = d_counters_ + order[oi];
-                if (rec) {
-                    SHG_TRY_INT(rec->begin("resident<" + std::to_string(k.n) + ">", 32.0 * k.pt_steps, st));
-                    SHG_CUDA(launch_resident(k.n, d_desc_, list, k.count, counter, k.max_clusters, st));
-                    SHG_TRY_INT(rec->end(st));
-                } else {
-                    cudaStream_t ss = side_streams_[oi];
-                    SHG_CUDA(cudaStreamWaitEvent(ss, fork_event_, 0));
-                    SHG_CUDA(launch_resident(k.n, d_desc_, list, k.count, counter, k.max_clusters, ss));
-                    SHG_CUDA(cudaEventRecord(side_events_[oi], ss));
-                }
-            }
-            if (!rec)
-                for (int oi = 0; oi < (int)order.size(); ++oi) SHG_CUDA(cudaStreamWaitEvent(st, side_events_[oi], 0));
+        SHG_CUDA(cudaMemsetAsync(d_counters_, 0, 64 * sizeof(int), st));
+        // classes in descending grid size; concurrently on side streams unless timed
+        std::vector<int> order(classes_.size());
+        for (int i = 0; i < (int)order.size(); ++i) order[i] = i;
+        std::sort(order.begin(), order.end(), [&](int x, int y) { return classes_[x].n > classes_[y].n; });
+        if (rec || order.size() == 1) {
+            for (int ci : order) SHG_TRY_INT(enqueue_class(ci, st, rec));
             return SHG_OK;
         }
-        for (const auto &k : classes_) {
-            const int K = k.steps[0];
-            const int *list = d_lists_ + k.offset;
-            const double nn = (double)k.n * k.n;
-            const std::string rn = "rows<" + std::to_string(k.n) + ">", cn = "cols<" + std::to_string(k.n) + ">";
-            for (int s = 0; s <= K; ++s) {
-                // solves with nsteps >= s run the row pass, nsteps >= s + 1 the column pass
-                const int nr = count_at_least(k.steps, s), nc = count_at_least(k.steps, s + 1);
-                // algorithmic bytes: both fields read and written (rows), plus both
-                // propagators read (columns)
-                if (rec) SHG_TRY_INT(rec->begin(rn, 32.0 * nn * nr, st));
-                SHG_CUDA(launch_rows(k.n, d_desc_, list, nr, s, st));
+        SHG_CUDA(cudaEventRecord(fork_event_, st));
+        for (int oi = 0; oi < (int)order.size(); ++oi) {
+            cudaStream_t ss = side_streams_[oi];
+            SHG_CUDA(cudaStreamWaitEvent(ss, fork_event_, 0));
+            SHG_TRY_INT(enqueue_class(order[oi], ss, nullptr));
+            SHG_CUDA(cudaEventRecord(side_events_[oi], ss));
+        }
+        for (int oi = 0; oi < (int)order.size(); ++oi) SHG_CUDA(cudaStreamWaitEvent(st, side_events_[oi], 0));
+        return SHG_OK;
+    }
+
+    // The march of class ci on `st` with its current schedule.
+    int enqueue_class(int ci, cudaStream_t st, Recorder *rec) {
+        const Class &k = classes_[ci];
+        const int *list = d_lists_ + k.offset;
+        if (k.resident) {
+            int *counter = d_counters_ + ci;
+            if (rec) SHG_TRY_INT(rec->begin("resident<" + std::to_string(k.n) + ">", 32.0 * k.pt_steps, st));
+            SHG_CUDA(launch_resident(k.n, k.var, d_desc_, list, k.count, counter, k.max_clusters, st));
+            if (rec) SHG_TRY_INT(rec->end(st));
+            return SHG_OK;
+        }
+        const int K = k.steps[0];
+        const double nn = (double)k.n * k.n;
+        const std::string rn = "rows<" + std::to_string(k.n) + ">", cn = "cols<" + std::to_string(k.n) + ">";
+        for (int s = 0; s <= K; ++s) {
+            // solves with nsteps >= s run the row pass, nsteps >= s + 1 the column pass
+            const int nr = count_at_least(k.steps, s), nc = count_at_least(k.steps, s + 1);
+            // algorithmic bytes: both fields read and written (rows), plus both
+            // propagators read (columns)
+            if (rec) SHG_TRY_INT(rec->begin(rn, 32.0 * nn * nr, st));
+            SHG_CUDA(launch_rows(k.n, d_desc_, list, nr, s, st));
+            if (rec) SHG_TRY_INT(rec->end(st));
+            if (nc > 0) {
+                if (rec) SHG_TRY_INT(rec->begin(cn, 48.0 * nn * nc, st));
+                SHG_CUDA(launch_cols(k.n, d_desc_, list, nc, st));
                 if (rec) SHG_TRY_INT(rec->end(st));
-                if (nc > 0) {
-                    if (rec) SHG_TRY_INT(rec->begin(cn, 48.0 * nn * nc, st));
-                    SHG_CUDA(launch_cols(k.n, d_desc_, list, nc, st));
-                    if (rec) SHG_TRY_INT(rec->end(st));
-                }
             }
         }
         return SHG_OK;
@@ -598,7 +772,6 @@ class Batch {
     bool desc_dirty_ = true;
     cudaGraphExec_t graph_exec_ = nullptr;
     cudaStream_t capture_stream_ = nullptr;
-    bool resident_ = true;
     int *d_counters_ = nullptr;
     std::vector<cudaStream_t> side_streams_;
     std::vector<cudaEvent_t> side_events_;
@@ -1206,6 +1379,35 @@ int shg_batch_launch_count(shg_batch *b, int *launches) {
     }
     *launches = b->batch.launch_count();
     return SHG_OK;
+}
+
+int shg_batch_autotune(shg_batch *b, void *stream) {
+    if (!b) {
+        set_error("null argument");
+        return SHG_ERR_INVALID;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    SHG_TRY_INT(b->batch.tune(st));
+    SHG_CUDA(cudaStreamSynchronize(st));
+    return SHG_OK;
+}
+
+int shg_batch_set_schedule(shg_batch *b, int n, int resident, int cluster_size, int ctas_per_sm) {
+    if (!b) {
+        set_error("null argument");
+        return SHG_ERR_INVALID;
+    }
+    return b->batch.set_schedule(n, resident, cluster_size, ctas_per_sm);
+}
+
+int shg_batch_schedule(shg_batch *b, char *buf, int len) {
+    if (!b || !buf || len <= 0) {
+        set_error("null argument");
+        return SHG_ERR_INVALID;
+    }
+    const std::string s = b->batch.schedule();
+    std::snprintf(buf, (size_t)len, "%s", s.c_str());
+    return (int)s.size() < len ? SHG_OK : SHG_ERR_INVALID;
 }
 
 int shg_dft2d_device(int n, int sign, const void *in, void *out, void *stream) {

@@ -16,12 +16,18 @@ const float2 *twiddle_symbol_address_march();
 const float2 *twiddle_symbol_address_thermal();
 const float2 *twiddle_symbol_address_adjoint();
 const float2 *twiddle_symbol_address_resident();
+const float2 *twiddle_symbol_address_resident128();
+const float2 *twiddle_symbol_address_resident256();
 
-// shg_march_v1.cu (resident march)
-cudaError_t prepare_resident(int n, int *max_clusters);
-cudaError_t launch_resident(int n, const InstDesc *inst, const int *list, int njobs, int *counter, int max_clusters,
-                            cudaStream_t st);
-int resident_cluster_size(int n);
+// shg_march_v1.cu (resident march): variants (cluster size, CTAs per SM) per grid size
+struct ResidentVariant {
+    int cs, minb;
+};
+int resident_variants(int n, ResidentVariant *out, int max_out);
+ResidentVariant resident_default(int n);
+cudaError_t prepare_resident(int n, ResidentVariant v, int *max_clusters);
+cudaError_t launch_resident(int n, ResidentVariant v, const InstDesc *inst, const int *list, int njobs, int *counter,
+                            int max_clusters, cudaStream_t st);
 
 // shg_march.cu
 cudaError_t launch_setup(const InstDesc *inst, int n_inst, int max_nn, int max_nz, cudaStream_t st);

@@ -1,7 +1,7 @@
 // Resident z-march: every solve keeps both fields in shared memory for its whole march.
 //
-// A solve of N x N points is owned by a thread-block cluster of CS CTAs (CS = 1 for
-// N <= 64, 2 for N = 128, 8 for N = 256); CTA r of the cluster holds rows
+// A solve of N x N points is owned by a thread-block cluster of CS CTAs (variants: CS = 1
+// or 2 for N = 64, 2 or 4 for N = 128, 8 or 16 for N = 256); CTA r of the cluster holds rows
 // [r*R, (r+1)*R), R = N / CS, of the pump and SH fields. Per SSFM step:
 //   row phase (local):   forward FFT along x finishing step s-1, RK4(z_{s-1}),
 //                        [capture at the top of slice nz-1], RK4(z_s), backward FFT;
@@ -19,280 +19,67 @@
 // The kernel is persistent: each cluster takes solves of its size class from a queue
 // (an atomic counter over the class list, ordered by work, largest first) until none is
 // left. No cluster waits on another, so a cluster that starts late only finds fewer solves.
-#include <cooperative_groups.h>
+//
+// The kernel template lives in shg_resident.cuh and is instantiated per grid size in
+// shg_resident_{64,128,256}.cu; this file lists the variants (cluster size CS and CTAs
+// per SM MINB) that the batch schedule's autotuner times, and dispatches to them.
 #include <cuda_runtime.h>
 
 #include "shg_internal.h"
-#include "shg_march.cuh"
-
-namespace cg = cooperative_groups;
 
 namespace shg {
 
-const float2 *twiddle_symbol_address_resident() {
-    void *p = nullptr;
-    cudaGetSymbolAddress(&p, g_twiddle);
-    return static_cast<const float2 *>(p);
-}
+cudaError_t prepare_resident_small(int n, int cs, int minb, int *max_clusters);
+cudaError_t launch_resident_small(int n, int cs, int minb, const InstDesc *inst, const int *list, int njobs,
+                                  int *counter, int max_clusters, cudaStream_t st);
+cudaError_t prepare_resident_128(int cs, int minb, int *max_clusters);
+cudaError_t launch_resident_128(int cs, int minb, const InstDesc *inst, const int *list, int njobs, int *counter,
+                                int max_clusters, cudaStream_t st);
+cudaError_t prepare_resident_256(int cs, int minb, int *max_clusters);
+cudaError_t launch_resident_256(int cs, int minb, const InstDesc *inst, const int *list, int njobs, int *counter,
+                                int max_clusters, cudaStream_t st);
 
-template <int N>
-struct Resident;
-template <> struct Resident<16> { static constexpr int CS = 1; };
-template <> struct Resident<32> { static constexpr int CS = 1; };
-template <> struct Resident<64> { static constexpr int CS = 1; };
-template <> struct Resident<128> { static constexpr int CS = 2; };
-template <> struct Resident<256> { static constexpr int CS = 8; };
-
-template <int N>
-struct ResShape {
-    static constexpr int CS = Resident<N>::CS;
-    static constexpr int G = LineShape<N>::G, E = N / G;
-    static constexpr int R = N / CS;             // rows (and columns) per CTA
-    static constexpr int THREADS = R * G;
-    static constexpr int SC_ROW = LineScratch<N, G>::SIZE;
-    static constexpr int FIELD = R * N;          // complex values per field per CTA
-    static constexpr int SCR = (R * SC_ROW > R * N) ? R * SC_ROW : R * N;
-    static constexpr size_t SMEM = (size_t)(2 * FIELD + SCR) * sizeof(float2);
-};
-
-template <int CS>
-__device__ __forceinline__ void cluster_barrier() {
-    if constexpr (CS > 1)
-        cg::this_cluster().sync();
-    else
-        __syncthreads();
-}
-
-__device__ __forceinline__ void block_add_double_res(double v, double *dst) {
-    __shared__ double red[32];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    __syncthreads();
-    if (l == 0) red[w] = v;
-    __syncthreads();
-    if (w == 0) {
-        v = (l < (int)(blockDim.x >> 5)) ? red[l] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (l == 0 && v != 0.0) atomicAdd(dst, v);
-    }
-}
-
-template <int N>
-__global__ void __launch_bounds__(ResShape<N>::THREADS, 1)
-    k_march_resident(const InstDesc *__restrict__ inst, const int *__restrict__ list, int njobs, int *counter) {
-    using Sh = ResShape<N>;
-    constexpr int CS = Sh::CS, G = Sh::G, E = Sh::E, R = Sh::R, FIELD = Sh::FIELD, SC_ROW = Sh::SC_ROW;
-    extern __shared__ float2 smem[];
-    float2 *sP = smem, *sS = smem + FIELD, *scr = smem + 2 * FIELD;
-    __shared__ int job_s;
-    const float2 *__restrict__ tab = g_twiddle + N;
-    int rank = 0;
-    if constexpr (CS > 1) rank = (int)cg::this_cluster().block_rank();
-    const int tid = threadIdx.x;
-    // row-phase roles
-    const int line = tid / G, t = tid % G;
-    float2 *rsc = scr + line * SC_ROW;
-    // column-phase roles
-    const int cc = tid % R, ct = tid / R;
-
-    for (;;) {
-        if (rank == 0 && tid == 0) job_s = atomicAdd(counter, 1);
-        cluster_barrier<CS>();
-        int job;
-        if constexpr (CS > 1)
-            job = *cg::this_cluster().map_shared_rank(&job_s, 0);
-        else
-            job = job_s;
-        // every CTA has read the job index before rank 0 may exit or overwrite it
-        cluster_barrier<CS>();
-        if (job >= njobs) break;
-        const InstDesc &d = inst[list[job]];
-        // load this CTA's rows of both fields
-        {
-            const float4 *gP = reinterpret_cast<const float4 *>(d.P + (size_t)rank * FIELD);
-            const float4 *gS = reinterpret_cast<const float4 *>(d.S + (size_t)rank * FIELD);
-            float4 *lP = reinterpret_cast<float4 *>(sP), *lS = reinterpret_cast<float4 *>(sS);
-            for (int i = tid; i < FIELD / 2; i += Sh::THREADS) {
-                lP[i] = gP[i];
-                lS[i] = gS[i];
-            }
-        }
-        __syncthreads();
-        const int K = d.nsteps;
-        for (int s = 0; s <= K; ++s) {
-            // ---- row phase (local rows)
-            {
-                float2 *rowP = sP + line * N, *rowS = sS + line * N;
-                float2 vp[E], vs[E];
-#pragma unroll
-                for (int j = 0; j < E; ++j) {
-                    vp[j] = rowP[t + G * j];
-                    vs[j] = rowS[t + G * j];
-                }
-                if (s == 0) {
-                    const float4 c = d.stepc[0];
-#pragma unroll
-                    for (int j = 0; j < E; ++j) rk4_point(vp[j], vs[j], c, d);
-                    fft_nat_to_spec<N, G, +1>(vp, t, rsc, tab);
-                    fft_nat_to_spec<N, G, +1>(vs, t, rsc, tab);
-                    __syncwarp();
-#pragma unroll
-                    for (int r = 0; r < E; ++r) {
-                        const int k = spec_index<N, G>(t, r);
-                        rowP[k] = vp[r];
-                        rowS[k] = vs[r];
-                    }
-                } else {
-                    fft_nat_to_spec<N, G, -1>(vp, t, rsc, tab);
-                    fft_nat_to_spec<N, G, -1>(vs, t, rsc, tab);
-                    const float4 c1 = d.stepc[s - 1];
-#pragma unroll
-                    for (int r = 0; r < E; ++r) rk4_point(vp[r], vs[r], c1, d);
-                    if (d.slices && s < d.nz) {
-                        float2 *sl = d.slices + (size_t)s * 2 * N * N + (size_t)(rank * R + line) * N;
-#pragma unroll
-                        for (int r = 0; r < E; ++r) {
-                            const int k = spec_index<N, G>(t, r);
-                            sl[k] = vp[r];
-                            sl[(size_t)N * N + k] = vs[r];
-                        }
-                    }
-                    if (s == K) {
-                        const size_t base = (size_t)(rank * R + line) * N;
-                        double aS = 0.0, aP = 0.0;
-#pragma unroll
-                        for (int r = 0; r < E; ++r) {
-                            const int k = spec_index<N, G>(t, r);
-                            d.Pout[base + k] = vp[r];
-                            d.Sout[base + k] = vs[r];
-                            aS += (double)vs[r].x * vs[r].x + (double)vs[r].y * vs[r].y;
-                            aP += (double)vp[r].x * vp[r].x + (double)vp[r].y * vp[r].y;
-                        }
-                        block_add_double_res(aS, d.acc + 1);
-                        block_add_double_res(aP, d.acc + 2);
-                    } else {
-                        const float4 c2 = d.stepc[s];
-#pragma unroll
-                        for (int r = 0; r < E; ++r) rk4_point(vp[r], vs[r], c2, d);
-                        fft_spec_to_nat<N, G, +1>(vp, t, rsc, tab);
-                        fft_spec_to_nat<N, G, +1>(vs, t, rsc, tab);
-#pragma unroll
-                        for (int j = 0; j < E; ++j) {
-                            rowP[t + G * j] = vp[j];
-                            rowS[t + G * j] = vs[j];
-                        }
-                    }
-                }
-            }
-            if (s == K) break;
-            cluster_barrier<CS>();
-            // ---- column phase: columns [rank*R, rank*R + R)
-            {
-                const int x = rank * R + cc;
-#pragma unroll 1
-                for (int f = 0; f < 2; ++f) {
-                    float2 *F = f == 0 ? sP : sS;
-                    const float2 *__restrict__ H = f == 0 ? d.Hp : d.Hs;
-                    auto at = [&](int j) -> float2 * {
-                        const int y = ct + G * j;
-                        float2 *p = F + (y % R) * N + x;
-                        if constexpr (CS > 1) p = cg::this_cluster().map_shared_rank(p, y / R);
-                        return p;
-                    };
-                    float2 v[E];
-#pragma unroll
-                    for (int j = 0; j < E; ++j) v[j] = *at(j);
-                    fft_nat_to_spec<N, G, +1, true, R, G>(v, ct, scr + cc, tab);
-#pragma unroll
-                    for (int r = 0; r < E; ++r) {
-                        const int k = spec_index<N, G>(ct, r);
-                        v[r] = c_mul(v[r], __ldg(H + (size_t)k * N + x));
-                    }
-                    fft_spec_to_nat<N, G, -1, true, R, G>(v, ct, scr + cc, tab);
-#pragma unroll
-                    for (int j = 0; j < E; ++j) *at(j) = v[j];
-                    __syncthreads();  // scratch reuse by the second field
-                }
-            }
-            cluster_barrier<CS>();
-        }
-        // The next job's loads touch only this CTA's shared memory; all remote accesses of
-        // this job ended before the last cluster barrier.
-    }
-}
-
-template <int N>
-static cudaLaunchConfig_t resident_config(cudaLaunchAttribute *attr, cudaStream_t st) {
-    using Sh = ResShape<N>;
-    cudaLaunchConfig_t cfg = {};
-    cfg.blockDim = dim3(Sh::THREADS, 1, 1);
-    cfg.dynamicSmemBytes = Sh::SMEM;
-    cfg.stream = st;
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = Sh::CS;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cfg;
-}
-
-// Once per device, outside any stream capture: shared-memory limit and the number of
-// clusters that fit at once.
-template <int N>
-static cudaError_t prepare_resident_t(int *max_clusters) {
-    using Sh = ResShape<N>;
-    cudaError_t e =
-        cudaFuncSetAttribute(k_march_resident<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Sh::SMEM);
-    if (e != cudaSuccess) return e;
-    cudaLaunchAttribute attr[1];
-    cudaLaunchConfig_t cfg = resident_config<N>(attr, nullptr);
-    cfg.gridDim = dim3(Sh::CS, 1, 1);
-    return cudaOccupancyMaxActiveClusters(max_clusters, k_march_resident<N>, &cfg);
-}
-
-template <int N>
-static cudaError_t launch_resident_t(const InstDesc *inst, const int *list, int njobs, int *counter, int max_clusters,
-                                     cudaStream_t st) {
-    using Sh = ResShape<N>;
-    cudaLaunchAttribute attr[1];
-    cudaLaunchConfig_t cfg = resident_config<N>(attr, st);
-    int clusters = max_clusters;
-    if (clusters > njobs) clusters = njobs;
-    if (clusters < 1) clusters = 1;
-    cfg.gridDim = dim3(clusters * Sh::CS, 1, 1);
-    return cudaLaunchKernelEx(&cfg, k_march_resident<N>, inst, list, njobs, counter);
-}
-
-cudaError_t launch_resident(int n, const InstDesc *inst, const int *list, int njobs, int *counter, int max_clusters,
-                            cudaStream_t st) {
+int resident_variants(int n, ResidentVariant *out, int max_out) {
+    static const ResidentVariant v16[] = {{1, 1}};
+    static const ResidentVariant v64[] = {{1, 1}, {1, 2}, {2, 2}, {2, 4}};
+    static const ResidentVariant v128[] = {{2, 1}, {4, 1}, {4, 2}};
+    static const ResidentVariant v256[] = {{8, 1}, {16, 1}, {16, 2}};
+    const ResidentVariant *v = nullptr;
+    int c = 0;
     switch (n) {
-        case 16: return launch_resident_t<16>(inst, list, njobs, counter, max_clusters, st);
-        case 32: return launch_resident_t<32>(inst, list, njobs, counter, max_clusters, st);
-        case 64: return launch_resident_t<64>(inst, list, njobs, counter, max_clusters, st);
-        case 128: return launch_resident_t<128>(inst, list, njobs, counter, max_clusters, st);
-        case 256: return launch_resident_t<256>(inst, list, njobs, counter, max_clusters, st);
-        default: return cudaErrorInvalidValue;
-    }
-}
-
-cudaError_t prepare_resident(int n, int *max_clusters) {
-    switch (n) {
-        case 16: return prepare_resident_t<16>(max_clusters);
-        case 32: return prepare_resident_t<32>(max_clusters);
-        case 64: return prepare_resident_t<64>(max_clusters);
-        case 128: return prepare_resident_t<128>(max_clusters);
-        case 256: return prepare_resident_t<256>(max_clusters);
-        default: return cudaErrorInvalidValue;
-    }
-}
-
-int resident_cluster_size(int n) {
-    switch (n) {
-        case 16: case 32: case 64: return 1;
-        case 128: return 2;
-        case 256: return 8;
+        case 16: case 32: v = v16; c = 1; break;
+        case 64: v = v64; c = 4; break;
+        case 128: v = v128; c = 3; break;
+        case 256: v = v256; c = 3; break;
         default: return 0;
+    }
+    for (int i = 0; i < c && i < max_out; ++i) out[i] = v[i];
+    return c < max_out ? c : max_out;
+}
+
+ResidentVariant resident_default(int n) {
+    ResidentVariant v{1, 1};
+    resident_variants(n, &v, 1);
+    return v;
+}
+
+cudaError_t prepare_resident(int n, ResidentVariant v, int *max_clusters) {
+    switch (n) {
+        case 16: case 32: case 64: return prepare_resident_small(n, v.cs, v.minb, max_clusters);
+        case 128: return prepare_resident_128(v.cs, v.minb, max_clusters);
+        case 256: return prepare_resident_256(v.cs, v.minb, max_clusters);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_resident(int n, ResidentVariant v, const InstDesc *inst, const int *list, int njobs, int *counter,
+                            int max_clusters, cudaStream_t st) {
+    switch (n) {
+        case 16: case 32: case 64:
+            return launch_resident_small(n, v.cs, v.minb, inst, list, njobs, counter, max_clusters, st);
+        case 128: return launch_resident_128(v.cs, v.minb, inst, list, njobs, counter, max_clusters, st);
+        case 256: return launch_resident_256(v.cs, v.minb, inst, list, njobs, counter, max_clusters, st);
+        default: return cudaErrorInvalidValue;
     }
 }
 

@@ -241,6 +241,21 @@ class Sweep:
         check(lib().shg_batch_io_bytes(self._b, C.byref(a), C.byref(b)), "shg_batch_io_bytes")
         return a.value, b.value
 
+    def autotune(self, stream=None):
+        """Time the schedules of every grid-size class now (outside any capture)."""
+        check(lib().shg_batch_autotune(self._b, stream), "shg_batch_autotune")
+
+    def set_schedule(self, n, resident=True, cluster_size=1, ctas_per_sm=1):
+        """Fix the schedule of the grid-n class (streaming, or a resident variant)."""
+        check(lib().shg_batch_set_schedule(self._b, int(n), int(bool(resident)), int(cluster_size),
+                                           int(ctas_per_sm)), "shg_batch_set_schedule")
+
+    def schedule(self) -> str:
+        """The schedule chosen per grid-size class, with the autotuner's trial times."""
+        buf = C.create_string_buffer(8192)
+        check(lib().shg_batch_schedule(self._b, buf, len(buf)), "shg_batch_schedule")
+        return buf.value.decode()
+
     def launch_count(self) -> int:
         v = C.c_int()
         check(lib().shg_batch_launch_count(self._b, C.byref(v)), "shg_batch_launch_count")

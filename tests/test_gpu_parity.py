@@ -138,19 +138,43 @@ def test_errors_are_reported():
         s.cwes(50.0)
 
 
-def test_resident_march_equals_streaming_march(monkeypatch):
-    """The resident (shared-memory) march runs the same arithmetic as the streaming
-    row/column kernels: identical output fields for every size class."""
+RESIDENT_VARIANTS = {64: [(1, 1), (1, 2), (2, 2), (2, 4)], 128: [(2, 1), (4, 1), (4, 2)],
+                     256: [(8, 1), (16, 1), (16, 2)]}
+
+
+def test_every_schedule_gives_identical_fields():
+    """Every resident variant (cluster size, CTAs per SM) runs the same arithmetic as the
+    streaming row/column kernels: identical output fields for every size class; the
+    autotuner's choice too."""
+    from shg_focused_gaussian_beams_gb300._lib import ShgError
     insts = W.config_sweep(count=512, seed=77)
     pick = [i for i in insts if i.nx == 64][:5] + [i for i in insts if i.nx == 128][:4] + \
         [i for i in insts if i.nx == 256][:3]
     pick = [W.Instance(**{**i.as_dict(), "nz": min(i.nz, 60)}) for i in pick]
-    a = Sweep(pick, crystal=W.CRYSTAL_QPM50)
-    eta_a, fa = a.run(with_fields=True)
-    monkeypatch.setenv("SHG_MARCH", "streaming")
-    b = Sweep(pick, crystal=W.CRYSTAL_QPM50)
-    eta_b, fb = b.run(with_fields=True)
-    assert a.launch_count() < b.launch_count()
-    for x, y in zip(fa, fb):
+    ref = Sweep(pick, crystal=W.CRYSTAL_QPM50)
+    for n in RESIDENT_VARIANTS:
+        ref.set_schedule(n, resident=False)
+    eta_r, fr = ref.run(with_fields=True)
+    ran = {n: 0 for n in RESIDENT_VARIANTS}
+    for k in range(4):
+        sw = Sweep(pick, crystal=W.CRYSTAL_QPM50)
+        for n, vs in RESIDENT_VARIANTS.items():
+            cs, mb = vs[min(k, len(vs) - 1)]
+            try:
+                sw.set_schedule(n, True, cs, mb)
+                ran[n] += 1
+            except ShgError as e:  # a variant that does not fit this device
+                assert "UNSUPPORTED" in str(e)
+                sw.set_schedule(n, resident=False)
+        eta, f = sw.run(with_fields=True)
+        for x, y in zip(f, fr):
+            assert np.array_equal(x, y)
+        np.testing.assert_allclose(eta, eta_r, rtol=1e-12, atol=0)
+    assert all(v > 0 for v in ran.values()), ran
+    at = Sweep(pick, crystal=W.CRYSTAL_QPM50)
+    at.autotune()
+    text = at.schedule()
+    assert "untuned" not in text and all(f"n={n}" in text for n in RESIDENT_VARIANTS), text
+    eta_t, ft = at.run(with_fields=True)
+    for x, y in zip(ft, fr):
         assert np.array_equal(x, y)
-    np.testing.assert_allclose(eta_a, eta_b, rtol=1e-12, atol=0)
