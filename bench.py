@@ -58,6 +58,11 @@ def workload(name, rank=0, world=1):
         # ncu-sized case: 64 solves of 256x256x100 (fields + propagators 200 MB > L2)
         insts = [W.plain_instance(256, 100, 10.0, 2.84, 50.0) for _ in range(64)]
         desc = {"workload": "64 plain solves 256x256x100 (profiling case)", "solves": len(insts)}
+    elif name == "resident256":
+        # ncu-sized case for the resident march: 38 solves of 256x256x100 (two per cluster slot)
+        insts = [W.plain_instance(256, 100, 10.0, 2.84, 50.0) for _ in range(38)]
+        desc = {"workload": "38 plain solves 256x256x100, resident cs16/2 schedule (profiling case)",
+                "solves": len(insts)}
     elif name == "plain128":
         insts = [W.config_plain_128()]
         desc = {"workload": "plain 128x128x200, P=10 W, xi=2.84, 50 C, window 16 w0", "solves": 1}
@@ -426,6 +431,8 @@ def run_ours(args):
     torch.cuda.set_device(local)
     insts, desc = workload(args.workload, rank, world)
     sw = Sweep(insts, crystal=W.CRYSTAL_QPM50, device=local)
+    if args.workload == "resident256":
+        sw.set_schedule(256, True, 16, 2)
     stream = torch.cuda.Stream()
     for _ in range(max(args.warmup, 3)):
         sw.run_async(stream.cuda_stream)
@@ -518,7 +525,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["sweep", "plain128", "rows256", "thermal256", "heat256", "adjoint256", "thermal_adjoint"],
+    ap.add_argument("--workload", choices=["sweep", "plain128", "rows256", "thermal256", "heat256", "adjoint256", "thermal_adjoint",
+                                              "resident256"],
                     default="sweep")
     args = ap.parse_args()
     if args.workload == "thermal256":
