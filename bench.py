@@ -209,13 +209,22 @@ def run_thermal_adjoint(args, count=64, n=256, nz=400, design_steps=20):
 
 
 def run_heat(args):
-    """Heat sweeps alone on the 256x256x400 THERMAL grid (profiling case)."""
+    """Heat sweeps alone on the 256x256x400 THERMAL grid: one sweep per launch and K = 2, 3,
+    4 sweeps per launch (temporal blocking); algorithmic bytes 12 per voxel and sweep."""
     inst = W.config_thermal_256()
-    per = heat_sweep_time(inst, max(args.steps, 1) * 100)
     vox = inst.nx * inst.ny * inst.nz
     peak, kind = measured_hbm()
-    print(json.dumps({"workload": "heat256", "ms_per_sweep": 1e3 * per, "GBps_algorithmic": 12.0 * vox / per / 1e9,
-                      "frac": 12.0 * vox / per / 1e9 / peak, "peak_source": kind}), flush=True)
+    out = {"workload": "heat256: Jacobi sweeps on 256x256x400, oven-surrounded", "peak": peak, "peak_source": kind}
+    for kind in args.heat_kinds.split(","):
+        os.environ["SHG_HEAT"] = kind
+        for lv in args.heat_levels.split(","):
+            os.environ["SHG_HEAT_TB"] = lv
+            per = heat_sweep_time(inst, max(args.steps, 1) * 96)
+            out[f"{kind}_levels_{lv}"] = {"ms_per_sweep": 1e3 * per, "GBps_algorithmic": 12.0 * vox / per / 1e9,
+                                          "frac": 12.0 * vox / per / 1e9 / peak}
+    os.environ.pop("SHG_HEAT_TB")
+    os.environ.pop("SHG_HEAT")
+    print(json.dumps(out), flush=True)
 
 
 def run_thermal(args):
@@ -252,7 +261,7 @@ def run_thermal(args):
             "config": {"workload": "thermal256: 256x256x400, P=30 W, xi=2.84, 2000x1000 um cross-section, "
                                    "oven-surrounded faces at a seeded U(45,55) C", "t_oven": inst.temp},
             "jacobi_counts": counts, "voxel_sweeps_per_s": vox * sweeps / t,
-            "roofline": {"bound": "hbm", "kernel": "k_heat<1>", "achieved": ach, "peak": peak, "unit": "GB/s",
+            "roofline": {"bound": "hbm", "kernel": "k_heat_ws<1,4> (one Jacobi sweep)", "achieved": ach, "peak": peak, "unit": "GB/s",
                          "frac": ach / peak, "peak_source": peak_kind, "ms_per_launch": 1e3 * per_sweep,
                          "algorithmic_bytes_per_launch": 12.0 * vox, "traffic": None,
                          "note": "CUDA events around 400 back-to-back sweeps on the launching stream"},
@@ -525,6 +534,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--heat-levels", default="1", help="heat256: sweeps per launch to time (1 = no blocking)")
+    ap.add_argument("--heat-kinds", default="ws8", help="heat256: single-sweep kernels to time (ws8, ws4, 25)")
     ap.add_argument("--workload", choices=["sweep", "plain128", "rows256", "thermal256", "heat256", "adjoint256", "thermal_adjoint",
                                               "resident256"],
                     default="sweep")

@@ -44,6 +44,13 @@ cudaError_t launch_init_temperature(float *T, int nx, int ny, int nz, float temp
                                     cudaStream_t st);
 cudaError_t launch_heat(float *Tf, const float *Ti, const float *QK, const HeatCoef &c, int nx, int ny, int nz,
                         int bc, cudaStream_t st);
+// K = levels sweeps in one launch (temporal blocking), levels in {2, 3, 4}; bit-identical
+// to K launch_heat calls. heat_levels(): the level count in use (SHG_HEAT_TB, default 1 =
+// no temporal blocking: the sweep is issue-bound, and the blocked form's redundant halo
+// updates cost more issue slots than its saved DRAM traffic on GB300).
+cudaError_t launch_heat_tb(float *Tf, const float *Ti, const float *QK, const HeatCoef &c, int nx, int ny, int nz,
+                           int bc, int levels, cudaStream_t st);
+int heat_levels();
 cudaError_t verify_fast_division(float d, float r, unsigned long long *d_count, unsigned long long *mismatches,
                                  cudaStream_t st);
 cudaError_t launch_sq_diff_sum(const float *Tf, const float *Ti, size_t n, double *out, cudaStream_t st);

@@ -198,6 +198,30 @@ __device__ __forceinline__ bool heat_voxel(const HeatCoef &c, int x, int y, int 
     return true;
 }
 
+// Interior voxel (Tfield.h:132) with the three divisions by dx^2, dy^2, dz^2 taken as
+// corrected products when all three numerators lie in the verified exponent range (one
+// combined test), else through div_const: bit-identical to heat_voxel's interior branch.
+__device__ __forceinline__ bool div_in_range(float a) {
+    return ((__float_as_uint(a) & 0x7f800000u) - (kDivExpLo << 23)) <= ((kDivExpHi - kDivExpLo) << 23);
+}
+
+__device__ __forceinline__ float interior_voxel(const HeatCoef &c, float xm, float xp, float ym, float yp, float zm,
+                                                float zp, float qk) {
+    const float sx = __fadd_rn(xp, xm), sy = __fadd_rn(yp, ym), sz = __fadd_rn(zp, zm);
+    float a, b, d;
+    if (c.fast_div && div_in_range(sx) && div_in_range(sy) && div_in_range(sz)) {
+        const float qa = sx * c.rdx2, qb = sy * c.rdy2, qd = sz * c.rdz2;
+        a = fmaf(fmaf(-qa, c.dx2, sx), c.rdx2, qa);
+        b = fmaf(fmaf(-qb, c.dy2, sy), c.rdy2, qb);
+        d = fmaf(fmaf(-qd, c.dz2, sz), c.rdz2, qd);
+    } else {
+        a = div_const(sx, c.dx2, c.rdx2, c.fast_div);
+        b = div_const(sy, c.dy2, c.rdy2, c.fast_div);
+        d = div_const(sz, c.dz2, c.rdz2, c.fast_div);
+    }
+    return __fmul_rn(c.L2, __fadd_rn(__fadd_rn(__fadd_rn(a, b), d), qk));
+}
+
 // 2.5D form of the same sweep: a 32x8 (x, y) tile marches a z range; each thread keeps
 // T(z-1), T(z), T(z+1) of its column in registers and reads its x / y neighbours from a
 // shared-memory copy of the current plane with a one-voxel halo. Every global load (the
@@ -269,6 +293,179 @@ __global__ void __launch_bounds__(HT_X * HT_Y) k_heat25(float *__restrict__ Tf, 
         a1 = a2;
         b0 = b1;
         b1 = b2;
+    }
+}
+
+// Warp-strip form of the same sweep: a warp owns a 32 (x) x RY (y) strip of columns and
+// marches a z range with no block-level synchronisation. Each lane keeps its column's RY
+// values of planes z-1, z, z+1 in registers (y neighbours inside the strip come from
+// registers, x neighbours from the adjacent lanes by shuffle); the two y-halo rows and the
+// 2 RY x-halo values (spread over lanes 0..RY-1 and 16..16+RY-1, then shuffled to lanes 0
+// and 31) are loaded per plane. All loads of plane z+1 (z+2 for the column values) are
+// issued before plane z is computed. Strips away from the x and y faces take the interior
+// formula for z-interior planes; other voxels go through heat_voxel.
+constexpr int WS_WARPS = 4;
+
+
+template <int BC, int RY, int MINB>
+__global__ void __launch_bounds__(32 * WS_WARPS, MINB) k_heat_ws(float *__restrict__ Tf, const float *__restrict__ Ti,
+                                                          const float *__restrict__ QK, const HeatCoef c, int nx,
+                                                          int ny, int nz, int zc) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int x0 = blockIdx.x * 32, x = x0 + lane;
+    const int y0 = (blockIdx.y * WS_WARPS + w) * RY;
+    if (y0 >= ny) return;  // uniform per warp; no block barrier below
+    const int z0 = blockIdx.z * zc, z1 = min(nz, z0 + zc);
+    const int sxy = nx * ny;
+    const bool xin = x < nx;
+    const bool wint = x0 >= 1 && x0 + 31 <= nx - 2 && y0 >= 1 && y0 + RY - 1 <= ny - 2;
+    // per-lane constants: column offset and validity of each row, the y-halo rows, and the
+    // x-halo role (left halo of row `lane` for lanes < RY, right halo of row lane - 16 for
+    // lanes 16 .. 16 + RY - 1)
+    const int b = y0 * nx + x;
+    unsigned rows = 0;
+#pragma unroll
+    for (int r = 0; r < RY; ++r) rows |= (xin && y0 + r < ny) ? 1u << r : 0u;
+    const bool lo_ok = xin && y0 >= 1, hi_ok = xin && y0 + RY < ny;
+    const int hy = lane < RY ? y0 + lane : (lane >= 16 && lane < 16 + RY) ? y0 + lane - 16 : -1;
+    const int hxx = lane < RY ? x0 - 1 : x0 + 32;
+    const bool h_ok = hy >= 0 && hy < ny && hxx >= 0 && hxx < nx;
+    const int hoff = h_ok ? hy * nx + hxx : 0;
+    auto ld = [&](const float *A, int z, bool ok, int off) -> float {
+        return (ok && z >= 0 && z < nz) ? A[z * sxy + off] : 0.f;
+    };
+    float m[RY], cc[RY], p[RY], q[RY];
+#pragma unroll
+    for (int r = 0; r < RY; ++r) {
+        const bool ok = rows >> r & 1u;
+        m[r] = ld(Ti, z0 - 1, ok, b + r * nx);
+        cc[r] = ld(Ti, z0, ok, b + r * nx);
+        p[r] = ld(Ti, z0 + 1, ok, b + r * nx);
+        q[r] = ld(QK, z0, ok, b + r * nx);
+    }
+    float ylo = ld(Ti, z0, lo_ok, b - nx), yhi = ld(Ti, z0, hi_ok, b + RY * nx);
+    float hx = ld(Ti, z0, h_ok, hoff);
+    for (int z = z0; z < z1; ++z) {
+        // loads for the next plane
+        float n[RY], qn[RY];
+        const bool more = z + 1 < z1;
+#pragma unroll
+        for (int r = 0; r < RY; ++r) {
+            const bool ok = more && (rows >> r & 1u);
+            n[r] = ld(Ti, z + 2, ok, b + r * nx);
+            qn[r] = ld(QK, z + 1, ok, b + r * nx);
+        }
+        const float ylon = ld(Ti, z + 1, more && lo_ok, b - nx);
+        const float yhin = ld(Ti, z + 1, more && hi_ok, b + RY * nx);
+        const float hxn = ld(Ti, z + 1, more && h_ok, hoff);
+        const bool zint = z > 0 && z < nz - 1;
+        float *out = Tf + z * sxy + b;
+#pragma unroll
+        for (int r = 0; r < RY; ++r) {
+            float xm = __shfl_up_sync(FULL, cc[r], 1), xp = __shfl_down_sync(FULL, cc[r], 1);
+            const float hl = __shfl_sync(FULL, hx, r), hr = __shfl_sync(FULL, hx, 16 + r);
+            if (lane == 0) xm = hl;
+            if (lane == 31) xp = hr;
+            const float ym = r == 0 ? ylo : cc[r - 1], yp = r == RY - 1 ? yhi : cc[r + 1];
+            if (wint && zint) {
+                out[r * nx] = interior_voxel(c, xm, xp, ym, yp, m[r], p[r], q[r]);
+            } else if (rows >> r & 1u) {
+                float v;
+                if (heat_voxel<BC>(c, x, y0 + r, z, nx, ny, nz, xm, xp, ym, yp, m[r], p[r], q[r], v))
+                    out[r * nx] = v;
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < RY; ++r) {
+            m[r] = cc[r];
+            cc[r] = p[r];
+            p[r] = n[r];
+            q[r] = qn[r];
+        }
+        ylo = ylon;
+        yhi = yhin;
+        hx = hxn;
+    }
+}
+
+// Temporal blocking: K sweeps per launch, bit-identical to K single sweeps. A block owns
+// a TB_X x TB_Y (x, y) tile and a z chunk of TB_ZC planes; its threads cover the tile with a
+// K-voxel halo (one (x, y) column each) and march z as a skewed pipeline: at step p the
+// input plane p enters a shared-memory ring (level 0) and level t = 1..K computes plane
+// p - 2t from level t-1's planes p-2t-1, p-2t, p-2t+1, all written in earlier steps, so one
+// barrier per step suffices (four-plane rings per level). Each level's region shrinks by
+// one voxel per side. Every voxel of every level runs heat_voxel, the same float operations
+// as a single sweep; voxels the reference never writes keep their value through the levels.
+// Q/k enters a 2K-plane ring one step before level 1 needs it. Global loads are issued two
+// steps ahead of their use. Global traffic per K sweeps: the input and Q/k with their
+// halos, the output once.
+constexpr int TB_X = 32, TB_Y = 16, TB_ZC = 50;
+
+template <int K>
+struct HeatTB {
+    static constexpr int RX = TB_X + 2 * K, RY = TB_Y + 2 * K, RP = RX * RY;
+    static constexpr size_t SMEM = (size_t)(4 * K + 2 * K) * RP * sizeof(float);
+};
+
+template <int BC, int K>
+__global__ void __launch_bounds__(HeatTB<K>::RP, 2) k_heat_tb(float *__restrict__ Tf, const float *__restrict__ Ti,
+                                                           const float *__restrict__ QK, const HeatCoef c, int nx,
+                                                           int ny, int nz) {
+    constexpr int RX = HeatTB<K>::RX, RY = HeatTB<K>::RY, RP = HeatTB<K>::RP;
+    extern __shared__ float hsm[];
+    float *ring = hsm;              // level t (0..K-1), plane z: ring + (4 t + z % 4) RP
+    float *qr = hsm + 4 * K * RP;   // Q/k plane z: qr + (z % 2K) RP
+    const int tid = threadIdx.x;
+    const int ix = tid % RX, iy = tid / RX;
+    const int gx = (int)blockIdx.x * TB_X - K + ix, gy = (int)blockIdx.y * TB_Y - K + iy;
+    const bool dom = gx >= 0 && gx < nx && gy >= 0 && gy < ny;
+    const bool colint = gx > 0 && gx < nx - 1 && gy > 0 && gy < ny - 1;
+    const int z0 = (int)blockIdx.z * TB_ZC, z1 = min(nz, z0 + TB_ZC);
+    const size_t sxy = (size_t)nx * ny;
+    const float *pT = Ti + (dom ? (size_t)gy * nx + gx : 0);
+    const float *pQ = QK + (dom ? (size_t)gy * nx + gx : 0);
+    float *pO = Tf + (dom ? (size_t)gy * nx + gx : 0);
+    for (int i = tid; i < 6 * K * RP; i += RP) hsm[i] = 0.f;
+    const int zlo0 = max(0, z0 - K), zhi0 = min(nz, z1 + K);
+    const int qlo = max(0, z0 - K + 1), qhi = min(nz, z1 + K - 1);  // planes level 1 computes
+    auto ldT = [&](int z) { return (dom && z >= zlo0 && z < zhi0) ? pT[(size_t)z * sxy] : 0.f; };
+    auto ldQ = [&](int z) { return (dom && z >= qlo && z < qhi) ? pQ[(size_t)z * sxy] : 0.f; };
+    float t1 = ldT(zlo0), t2 = ldT(zlo0 + 1);
+    float q1 = ldQ(zlo0 - 1), q2 = ldQ(zlo0);
+    __syncthreads();
+    for (int p = zlo0; p < z1 + 2 * K; ++p) {
+        // level 0 enters (plane p), Q/k plane p - 1 enters; both are first read next step
+        ring[(p & 3) * RP + tid] = t1;
+        if (p >= 1) qr[((p - 1) % (2 * K)) * RP + tid] = q1;
+        t1 = t2;
+        q1 = q2;
+        t2 = ldT(p + 2);
+        q2 = ldQ(p + 1);
+#pragma unroll
+        for (int t = 1; t <= K; ++t) {
+            const int zt = p - 2 * t;
+            const int zlo = max(0, z0 - (K - t)), zhi = min(nz, z1 + (K - t));
+            if (zt >= zlo && zt < zhi && dom && ix >= t && ix < RX - t && iy >= t && iy < RY - t) {
+                const float *pr = ring + 4 * (t - 1) * RP;
+                const float *cur = pr + (zt & 3) * RP;
+                const float zm = zt > 0 ? pr[((zt - 1) & 3) * RP + tid] : 0.f;
+                const float zp = zt + 1 < nz ? pr[((zt + 1) & 3) * RP + tid] : 0.f;
+                float out;
+                bool w = true;
+                if (colint && zt > 0 && zt < nz - 1)
+                    out = interior_voxel(c, cur[tid - 1], cur[tid + 1], cur[tid - RX], cur[tid + RX], zm, zp,
+                                         qr[(zt % (2 * K)) * RP + tid]);
+                else
+                    w = heat_voxel<BC>(c, gx, gy, zt, nx, ny, nz, cur[tid - 1], cur[tid + 1], cur[tid - RX],
+                                       cur[tid + RX], zm, zp, qr[(zt % (2 * K)) * RP + tid], out);
+                if (t < K)
+                    ring[(4 * t + (zt & 3)) * RP + tid] = w ? out : cur[tid];
+                else if (w)
+                    pO[(size_t)zt * sxy] = out;
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -459,10 +656,74 @@ cudaError_t launch_init_temperature(float *T, int nx, int ny, int nz, float temp
     return cudaGetLastError();
 }
 
+template <int BC, int K>
+static cudaError_t launch_heat_tb_t(float *Tf, const float *Ti, const float *QK, const HeatCoef &c, int nx, int ny,
+                                    int nz, cudaStream_t st) {
+    static unsigned long long done = 0;  // devices whose shared-memory limit is raised
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 64 && !(done >> dev & 1ull)) {
+        e = cudaFuncSetAttribute(k_heat_tb<BC, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)HeatTB<K>::SMEM);
+        if (e != cudaSuccess) return e;
+        done |= 1ull << dev;
+    }
+    dim3 grd((nx + TB_X - 1) / TB_X, (ny + TB_Y - 1) / TB_Y, (nz + TB_ZC - 1) / TB_ZC);
+    k_heat_tb<BC, K><<<grd, HeatTB<K>::RP, HeatTB<K>::SMEM, st>>>(Tf, Ti, QK, c, nx, ny, nz);
+    return cudaGetLastError();
+}
+
+int heat_levels() {
+    const char *e = std::getenv("SHG_HEAT_TB");
+    const int v = e ? std::atoi(e) : 1;
+    return (v == 2 || v == 3 || v == 4) ? v : 1;
+}
+
+cudaError_t launch_heat_tb(float *Tf, const float *Ti, const float *QK, const HeatCoef &c, int nx, int ny, int nz,
+                           int bc, int levels, cudaStream_t st) {
+    switch (levels * 2 + (bc != 0)) {
+        case 4: return launch_heat_tb_t<0, 2>(Tf, Ti, QK, c, nx, ny, nz, st);
+        case 5: return launch_heat_tb_t<1, 2>(Tf, Ti, QK, c, nx, ny, nz, st);
+        case 6: return launch_heat_tb_t<0, 3>(Tf, Ti, QK, c, nx, ny, nz, st);
+        case 7: return launch_heat_tb_t<1, 3>(Tf, Ti, QK, c, nx, ny, nz, st);
+        case 8: return launch_heat_tb_t<0, 4>(Tf, Ti, QK, c, nx, ny, nz, st);
+        case 9: return launch_heat_tb_t<1, 4>(Tf, Ti, QK, c, nx, ny, nz, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+// One sweep. SHG_HEAT selects the kernel (all bit-identical): ws4 (default; warp strips of
+// 4 rows, 8 blocks per SM), ws4b (same, 6 blocks per SM), ws8 (8-row strips), 25 (2.5D
+// shared-memory tile), simple (one thread per voxel). Measured at 256x256x400 on GB300:
+// 96.6, 100.0, 178, 108.6 us per sweep for the first four.
 cudaError_t launch_heat(float *Tf, const float *Ti, const float *QK, const HeatCoef &c, int nx, int ny, int nz,
                         int bc, cudaStream_t st) {
-    static const bool simple = std::getenv("SHG_HEAT") && std::string(std::getenv("SHG_HEAT")) == "simple";
-    if (!simple) {
+    const char *env = std::getenv("SHG_HEAT");
+    const std::string kind = env ? env : "ws4";
+    const bool fits32 = (long long)nx * ny * (nz + 3) < (1ll << 31);
+    if (fits32 && (kind == "ws8" || kind == "ws4" || kind == "ws4b")) {
+        const int ry = kind == "ws8" ? 8 : 4, zc = 20;
+        dim3 grd((nx + 31) / 32, (ny + ry * WS_WARPS - 1) / (ry * WS_WARPS), (nz + zc - 1) / zc);
+        const int blk = 32 * WS_WARPS;
+        if (kind == "ws8") {
+            if (bc == 0)
+                k_heat_ws<0, 8, 4><<<grd, blk, 0, st>>>(Tf, Ti, QK, c, nx, ny, nz, zc);
+            else
+                k_heat_ws<1, 8, 4><<<grd, blk, 0, st>>>(Tf, Ti, QK, c, nx, ny, nz, zc);
+        } else if (kind == "ws4") {
+            if (bc == 0)
+                k_heat_ws<0, 4, 8><<<grd, blk, 0, st>>>(Tf, Ti, QK, c, nx, ny, nz, zc);
+            else
+                k_heat_ws<1, 4, 8><<<grd, blk, 0, st>>>(Tf, Ti, QK, c, nx, ny, nz, zc);
+        } else {
+            if (bc == 0)
+                k_heat_ws<0, 4, 6><<<grd, blk, 0, st>>>(Tf, Ti, QK, c, nx, ny, nz, zc);
+            else
+                k_heat_ws<1, 4, 6><<<grd, blk, 0, st>>>(Tf, Ti, QK, c, nx, ny, nz, zc);
+        }
+        return cudaGetLastError();
+    }
+    if (kind != "simple" && fits32) {
         dim3 blk(HT_X, HT_Y, 1);
         dim3 grd((nx + HT_X - 1) / HT_X, (ny + HT_Y - 1) / HT_Y, (nz + HT_Z - 1) / HT_Z);
         if (bc == 0)

@@ -161,6 +161,11 @@ int ThermalSolve::sweeps(float t_inf, int n) {
         TH_TRY(enable_fast_division(hc_, st_));
         tinf_coef_ = t_inf;
     }
+    const int L = heat_levels();
+    for (; L > 1 && n >= L; n -= L) {
+        TH_CUDA(launch_heat_tb(T_[cur_ ^ 1], T_[cur_], qk_, hc_, n_, n_, nz_, bc_, L, st_));
+        cur_ ^= 1;
+    }
     for (int k = 0; k < n; ++k) {
         TH_CUDA(launch_heat(T_[cur_ ^ 1], T_[cur_], qk_, hc_, n_, n_, nz_, bc_, st_));
         cur_ ^= 1;
@@ -392,6 +397,11 @@ int shg_heat_sweeps_device(const shg_config *cfg, void *Ta, void *Tb, const void
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     TH_TRY(enable_fast_division(hc, st));
     float *a = static_cast<float *>(Ta), *b = static_cast<float *>(Tb);
+    const int L = heat_levels();
+    for (; L > 1 && nsweeps >= L; nsweeps -= L) {
+        TH_CUDA(launch_heat_tb(b, a, static_cast<const float *>(QK), hc, cfg->nx, cfg->ny, cfg->nz, bc, L, st));
+        std::swap(a, b);
+    }
     for (int k = 0; k < nsweeps; ++k) {
         TH_CUDA(launch_heat(b, a, static_cast<const float *>(QK), hc, cfg->nx, cfg->ny, cfg->nz, bc, st));
         std::swap(a, b);

@@ -56,6 +56,28 @@ def test_heat_sweeps_bitexact_vs_oracle_random():
     assert bits_equal(D, o.dk_thermal(T))
 
 
+@pytest.mark.parametrize("kind,levels", [("ws8", "1"), ("ws4", "1"), ("ws4b", "1"), ("25", "1"), ("simple", "1"), ("ws4", "2"),
+                                         ("ws4", "3"), ("ws4", "4")])
+def test_heat_kernels_bitexact(kind, levels, monkeypatch):
+    """Every heat-sweep kernel (warp strips of 8 or 4 rows, the 2.5D tile, the plain
+    kernel) and K sweeps per launch (temporal blocking) equal the reference's sweeps bit for
+    bit: a grid that no tile size divides, sweep counts around multiples of K, both BC modes."""
+    monkeypatch.setenv("SHG_HEAT", kind)
+    monkeypatch.setenv("SHG_HEAT_TB", levels)
+    n, nz = 40, 33
+    cfg = O.make_cfg(W.CRYSTAL_QPM50, n, n, nz, 600.0, 600.0)
+    o = O.Oracle(cfg)
+    rng = np.random.default_rng(11)
+    for bc in (0, 1):
+        T = o.init_temperature(48.0, 50.0, 46.5, bc)
+        T = (T + rng.normal(0, 0.05, T.shape)).astype(np.float32)
+        Q = (rng.random(T.shape) * 5e-9).astype(np.float32)
+        for ns in (1, 3, 4, 5, 9):
+            ref = o.heat_sweeps(T, Q, 25.0, ns, bc)
+            got = S.heat_sweeps(W.CRYSTAL_QPM50, T, Q, 25.0, ns, bc, lx=600.0, ly=600.0)
+            assert bits_equal(got, ref), (bc, ns)
+
+
 @pytest.mark.parametrize("name", ["thermal_topopen.npz", "thermal_oven.npz"])
 def test_thermal_run_matches_reference(name):
     g = golden(name)
