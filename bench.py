@@ -448,11 +448,16 @@ def run_ours(args):
     stream.synchronize()
     launches = sw.launch_count()
 
-    # device-resident timed region
+    # device-resident timed region; warm-up runs again once the clock sampler is up, so the
+    # GPU is at its working clocks (not ramping from idle) when timing starts
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier(world)
     torch.cuda.synchronize()
     with Clocks(local) as clk:
+        for _ in range(max(args.warmup, 3)):
+            sw.run_async(stream.cuda_stream)
+        stream.synchronize()
+        barrier(world)
         ev0.record(stream)
         for _ in range(args.steps):
             sw.run_async(stream.cuda_stream)
@@ -521,7 +526,8 @@ def run_ours(args):
                 "per_instance_gpu": per,
                 "batched_over_per_instance": {"solves_per_s": solves_s / world / per["solves_per_s"],
                                               "pt_steps_per_s": value / world / per["pt_steps_per_s"]},
-                "schedule": sw.schedule()}
+                "schedule": sw.schedule(),
+                "class_timeline_ms": sw.timeline()}
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist

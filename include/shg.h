@@ -157,7 +157,8 @@ int shg_batch_launch_count(shg_batch *b, int *launches);
 /* Schedule autotuner. Each grid-size class of the batch marches either as streaming
  * row/column launches or as one persistent resident launch (a thread-block cluster per
  * solve, fields in shared memory) in one of several (cluster size, CTAs per SM) variants.
- * Unless the environment variable SHG_MARCH is "streaming" or "resident", the first run
+ * Unless the environment variable SHG_MARCH is "streaming", "resident" (default variants)
+ * or lists a schedule per grid ("64:1/1,128:4/2,256:16/2", "64:streaming"), the first run
  * times every candidate on the class's own solves and keeps the fastest (cached per
  * device and class shape for the process). shg_batch_autotune does that now, outside any
  * stream capture; shg_batch_schedule writes the choices and trial times as text. */
@@ -168,6 +169,10 @@ int shg_batch_autotune(shg_batch *b, void *stream);
  * (8, 1), (16, 1), (16, 2)). SHG_ERR_UNSUPPORTED if the variant does not exist or fit. */
 int shg_batch_set_schedule(shg_batch *b, int n, int resident, int cluster_size, int ctas_per_sm);
 int shg_batch_schedule(shg_batch *b, char *buf, int len);
+/* Diagnostic: one concurrent run without a graph, with events around each grid-size class
+ * launched on its own stream as a run launches them; start_end[2k], start_end[2k+1] = start
+ * and end of class k (ascending grid order) in ms after the common start. */
+int shg_batch_timeline(shg_batch *b, double *start_end, int max_classes, int *n_classes, void *stream);
 
 /* Per-kernel timing of one un-captured run: CUDA events around every launch, summed per
  * kernel (name like "rows<128>"), with the algorithmic bytes those launches must move

@@ -252,18 +252,40 @@ class Batch {
             }
             classes_.push_back(c);
         }
-        // schedule per class: SHG_MARCH=streaming | resident (default variant) | auto (default:
-        // the autotuner picks at the first run)
+        // schedule per class from SHG_MARCH: "auto" (default: the autotuner picks at the first
+        // run), "streaming", "resident" (default variants), or a list "n:streaming" /
+        // "n:cs/minb" per grid (e.g. "64:1/1,128:4/2,256:16/2"; unlisted grids: autotuner)
         const char *mode = std::getenv("SHG_MARCH");
         const std::string m = mode ? mode : "auto";
         for (auto &c : classes_) {
             for (int k = 0; k < c.count; ++k) c.pt_steps += (double)c.n * c.n * c.steps[k];
-            c.tuned = m != "auto";
+            c.tuned = m == "streaming" || m == "resident";
             c.resident = m != "streaming";
-            if (c.resident) {
-                c.var = resident_default(c.n);
-                SHG_CUDA(prepare_resident(c.n, c.var, &c.max_clusters));
+            if (c.resident) c.var = resident_default(c.n);
+            const std::string key = std::to_string(c.n) + ":";
+            for (size_t pos = 0; pos < m.size();) {
+                size_t end = m.find(',', pos);
+                if (end == std::string::npos) end = m.size();
+                const std::string item = m.substr(pos, end - pos);
+                pos = end + 1;
+                if (item.compare(0, key.size(), key) != 0) continue;
+                const std::string v = item.substr(key.size());
+                int cs = 0, mb = 0;
+                if (v == "streaming") {
+                    c.resident = false;
+                    c.tuned = true;
+                } else if (std::sscanf(v.c_str(), "%d/%d", &cs, &mb) == 2) {
+                    ResidentVariant vs[8];
+                    const int nv = resident_variants(c.n, vs, 8);
+                    for (int i = 0; i < nv; ++i)
+                        if (vs[i].cs == cs && vs[i].minb == mb) {
+                            c.resident = true;
+                            c.var = vs[i];
+                            c.tuned = true;
+                        }
+                }
             }
+            if (c.resident) SHG_CUDA(prepare_resident(c.n, c.var, &c.max_clusters));
         }
         // resident march: class streams (largest solves first) and one job counter per class
         while ((int)side_streams_.size() < (int)classes_.size()) {
@@ -504,6 +526,41 @@ class Batch {
         }
         set_error("set_schedule: no class with that grid size");
         return SHG_ERR_INVALID;
+    }
+
+    // Concurrent run of the march as enqueue() launches it (classes on side streams, no
+    // graph) with events around each class: start / end of every class in ms after the
+    // common start, in class order.
+    int timeline(cudaStream_t st, std::vector<double> &se) {
+        SHG_TRY_INT(tune(st));
+        if (desc_dirty_) {
+            SHG_CUDA(cudaMemcpyAsync(d_desc_, desc_.data(), desc_.size() * sizeof(InstDesc), cudaMemcpyHostToDevice, st));
+            desc_dirty_ = false;
+        }
+        SHG_TRY_INT(enqueue_inputs(st));
+        SHG_CUDA(launch_setup(d_desc_, (int)desc_.size(), max_nn_, max_nz_, st));
+        SHG_CUDA(cudaMemsetAsync(d_counters_, 0, 64 * sizeof(int), st));
+        const int nc = (int)classes_.size();
+        std::vector<cudaEvent_t> ev(2 * nc + 1);
+        for (auto &e : ev) SHG_CUDA(cudaEventCreate(&e));
+        SHG_CUDA(cudaEventRecord(ev[0], st));
+        for (int ci = 0; ci < nc; ++ci) {
+            cudaStream_t ss = side_streams_[ci];
+            SHG_CUDA(cudaStreamWaitEvent(ss, ev[0], 0));
+            SHG_CUDA(cudaEventRecord(ev[1 + 2 * ci], ss));
+            SHG_TRY_INT(enqueue_class(ci, ss, nullptr));
+            SHG_CUDA(cudaEventRecord(ev[2 + 2 * ci], ss));
+        }
+        for (int ci = 0; ci < nc; ++ci) SHG_CUDA(cudaStreamWaitEvent(st, ev[2 + 2 * ci], 0));
+        SHG_CUDA(cudaStreamSynchronize(st));
+        se.assign(2 * nc, 0.0);
+        for (int i = 0; i < 2 * nc; ++i) {
+            float ms = 0.f;
+            SHG_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1 + i]));
+            se[i] = ms;
+        }
+        for (auto &e : ev) cudaEventDestroy(e);
+        return SHG_OK;
     }
 
     // One line per class: grid, solves, chosen schedule and the trial times (ms).
@@ -1389,6 +1446,18 @@ int shg_batch_autotune(shg_batch *b, void *stream) {
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     SHG_TRY_INT(b->batch.tune(st));
     SHG_CUDA(cudaStreamSynchronize(st));
+    return SHG_OK;
+}
+
+int shg_batch_timeline(shg_batch *b, double *start_end, int max_classes, int *n_classes, void *stream) {
+    if (!b || !start_end || !n_classes) {
+        set_error("null argument");
+        return SHG_ERR_INVALID;
+    }
+    std::vector<double> se;
+    SHG_TRY_INT(b->batch.timeline(static_cast<cudaStream_t>(stream), se));
+    *n_classes = (int)se.size() / 2;
+    for (int i = 0; i < (int)se.size() && i < 2 * max_classes; ++i) start_end[i] = se[i];
     return SHG_OK;
 }
 

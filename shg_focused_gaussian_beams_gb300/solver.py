@@ -250,6 +250,13 @@ class Sweep:
         check(lib().shg_batch_set_schedule(self._b, int(n), int(bool(resident)), int(cluster_size),
                                            int(ctas_per_sm)), "shg_batch_set_schedule")
 
+    def timeline(self, stream=None):
+        """[(start_ms, end_ms)] per grid-size class of one concurrent run (diagnostic)."""
+        out = (C.c_double * 64)()
+        n = C.c_int()
+        check(lib().shg_batch_timeline(self._b, out, 32, C.byref(n), stream), "shg_batch_timeline")
+        return [(out[2 * k], out[2 * k + 1]) for k in range(n.value)]
+
     def schedule(self) -> str:
         """The schedule chosen per grid-size class, with the autotuner's trial times."""
         buf = C.create_string_buffer(8192)

@@ -178,3 +178,18 @@ def test_every_schedule_gives_identical_fields():
     eta_t, ft = at.run(with_fields=True)
     for x, y in zip(ft, fr):
         assert np.array_equal(x, y)
+
+
+def test_schedule_list_from_environment(monkeypatch):
+    """SHG_MARCH lists a schedule per grid; unlisted grids go to the autotuner."""
+    monkeypatch.setenv("SHG_MARCH", "64:streaming,128:4/2")
+    insts = W.config_sweep(count=512, seed=5)
+    pick = [i for i in insts if i.nx == 64][:2] + [i for i in insts if i.nx == 128][:2] + \
+        [i for i in insts if i.nx == 256][:1]
+    pick = [W.Instance(**{**i.as_dict(), "nz": min(i.nz, 30)}) for i in pick]
+    sw = Sweep(pick, crystal=W.CRYSTAL_QPM50)
+    text = sw.schedule()
+    assert "n=64 solves=2: streaming" in text and "n=128 solves=2: resident cs=4 minb=2" in text
+    assert "n=256 solves=1: untuned" in text
+    sw.run()
+    assert "untuned" not in sw.schedule()
