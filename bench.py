@@ -266,6 +266,27 @@ def run_thermal(args):
                          "algorithmic_bytes_per_launch": 12.0 * vox, "traffic": None,
                          "note": "CUDA events around 400 back-to-back sweeps on the launching stream"},
             "clocks": clk.summary(), "efficiency": s.efficiency()}
+    # the workload's relative-residual stop rule (||dT|| / ||T|| < 1e-6, checked every 100 sweeps)
+    s.set_jacobi_rule(1e-6, check_every=100)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s.run(inst.power, inst.waist, inst.focal, inst.temp, inst.t_inf, inst.t1, inst.t2)
+    torch.cuda.synchronize()
+    line["relative_residual_mode"] = {"ms": 1e3 * (time.perf_counter() - t0), "jacobi_counts": s.jacobi_counts(),
+                                      "last_relative_residual": s.jacobi_residual(), "efficiency": s.efficiency()}
+    # CPU: the restatement's Jacobi sweep (the reference's loop) on this grid, one core
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    o = O.Oracle(O.make_cfg(W.CRYSTAL_QPM50, inst.nx, inst.ny, inst.nz, inst.lx, inst.ly))
+    T0 = o.init_temperature(inst.temp, inst.t1, inst.t2, inst.bc)
+    Q = np.full_like(T0, 1e-9)
+    t0 = time.perf_counter()
+    o.heat_sweeps(T0, Q, inst.t_inf, 3, inst.bc)
+    cpu = 3 * vox / (time.perf_counter() - t0)
+    line["cpu_baseline"] = {"value": cpu, "unit": "voxel-sweeps/s", "cores": 1, "kind": "port",
+                            "sample": "3 Jacobi sweeps of the 256x256x400 grid (the oracle restatement of "
+                                      "Tfield.h's sweep, single-threaded like the reference)"}
+    line["gpu_over_cpu_voxel_sweeps"] = vox / per_sweep / cpu
     print(json.dumps(line), flush=True)
 
 

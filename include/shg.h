@@ -106,6 +106,13 @@ int shg_set_poling_period(shg_handle *h, float lambda_qpm);
  * Solver.h:295-338 (-1 for iterations not run). */
 int shg_get_temperature(shg_handle *h, float *T);
 int shg_get_jacobi_counts(shg_handle *h, int *counts5);
+/* Jacobi stop rule of a THERMAL handle: rel_tol <= 0 (default) is the reference's rule
+ * (Solver.h:302-324: residual checked at sweep 0 and every 5000); rel_tol > 0 stops once
+ * ||T_k+1 - T_k|| / ||T_k+1|| < rel_tol (checked every check_every sweeps, at most
+ * max_sweeps per Jacobi solve), the relative-residual mode of the THERMAL workload.
+ * shg_get_jacobi_residual gives the last relative residual checked (-1 if none). */
+int shg_set_jacobi_rule(shg_handle *h, double rel_tol, int check_every, int max_sweeps);
+int shg_get_jacobi_residual(shg_handle *h, double *rel);
 /* Components on host buffers (NX = NY; grid from cfg): Tfield.h:31-110 initial
  * temperature; `nsweeps` sweeps of Tfield.h:113 (bc 0) or Tfield.h:224 (bc 1), each followed
  * by Tinic <- Tfinal (Solver.h:321), T updated in place, Q the heat source; and

@@ -76,6 +76,8 @@ SIGNATURES = {
     "shg_set_output_dir": (_i, [_vp, C.c_char_p]),
     "shg_get_temperature": (_i, [_vp, _pf]),
     "shg_get_jacobi_counts": (_i, [_vp, _pi]),
+    "shg_set_jacobi_rule": (_i, [_vp, C.c_double, _i, _i]),
+    "shg_get_jacobi_residual": (_i, [_vp, _pd]),
     "shg_init_temperature": (_i, [C.POINTER(Config), _f, _f, _f, _i, _pf]),
     "shg_heat_sweeps": (_i, [C.POINTER(Config), _pf, _pf, _f, _i, _i]),
     "shg_dk_thermal": (_i, [C.POINTER(Config), _pf, _pf, _pf, _pf]),

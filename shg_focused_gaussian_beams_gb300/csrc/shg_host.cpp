@@ -1265,6 +1265,30 @@ int shg_get_temperature(shg_handle *h, float *T) {
     return h->th->copy_temperature(T);
 }
 
+int shg_set_jacobi_rule(shg_handle *h, double rel_tol, int check_every, int max_sweeps) {
+    SHG_TRY(check_handle(h));
+    if (!h->th) {
+        set_error("shg_set_jacobi_rule: needs a thermal handle");
+        return SHG_ERR_STATE;
+    }
+    if (rel_tol > 0 && (check_every < 1 || max_sweeps < 1)) {
+        set_error("shg_set_jacobi_rule: check_every and max_sweeps must be positive");
+        return SHG_ERR_INVALID;
+    }
+    h->th->set_stop_rule(rel_tol, check_every, max_sweeps);
+    return SHG_OK;
+}
+
+int shg_get_jacobi_residual(shg_handle *h, double *rel) {
+    SHG_TRY(check_handle(h));
+    if (!h->th || !rel) {
+        set_error("shg_get_jacobi_residual: needs a thermal handle");
+        return SHG_ERR_STATE;
+    }
+    *rel = h->th->last_residual();
+    return SHG_OK;
+}
+
 int shg_get_jacobi_counts(shg_handle *h, int *counts) {
     SHG_TRY(check_handle(h));
     if (!h->th || !h->th->has_result() || !counts) {

@@ -54,6 +54,7 @@ int heat_levels();
 cudaError_t verify_fast_division(float d, float r, unsigned long long *d_count, unsigned long long *mismatches,
                                  cudaStream_t st);
 cudaError_t launch_sq_diff_sum(const float *Tf, const float *Ti, size_t n, double *out, cudaStream_t st);
+cudaError_t launch_sq_sums(const float *Tf, const float *Ti, size_t n, double *out2, cudaStream_t st);
 cudaError_t launch_sellmeier_tables(const float *T, float *NP, float *NS, float *DK, size_t n, float lp, float ls,
                                     float two_pi, float inv_lambda, cudaStream_t st);
 cudaError_t launch_rows_th(int n, const InstDesc *d, const ThermDesc &th, int s, cudaStream_t st);

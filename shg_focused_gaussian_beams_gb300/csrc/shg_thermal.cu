@@ -489,6 +489,39 @@ __global__ void k_sq_diff_sum(const float *__restrict__ Tf, const float *__restr
     }
 }
 
+// out[0] += sum (Tf - Ti)^2, out[1] += sum Tf^2 in FP64 (relative-residual stop rule).
+__global__ void k_sq_sums(const float *__restrict__ Tf, const float *__restrict__ Ti, size_t n, double *out) {
+    double a[2] = {0.0, 0.0};
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double f = Tf[i], d = f - (double)Ti[i];
+        a[0] += d * d;
+        a[1] += f * f;
+    }
+    __shared__ double red[32][2];
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    for (int k = 0; k < 2; ++k)
+        for (int o = 16; o > 0; o >>= 1) a[k] += __shfl_xor_sync(0xffffffffu, a[k], o);
+    if (l == 0) {
+        red[w][0] = a[0];
+        red[w][1] = a[1];
+    }
+    __syncthreads();
+    if (w == 0) {
+        for (int k = 0; k < 2; ++k) {
+            double v = l < (int)(blockDim.x >> 5) ? red[l][k] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (l == 0 && v != 0.0) atomicAdd(out + k, v);
+        }
+    }
+}
+
+cudaError_t launch_sq_sums(const float *Tf, const float *Ti, size_t n, double *out2, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(out2, 0, 2 * sizeof(double), st);
+    if (e != cudaSuccess) return e;
+    k_sq_sums<<<1216, 256, 0, st>>>(Tf, Ti, n, out2);
+    return cudaGetLastError();
+}
+
 // Crystal.h:116-132 in double with no contraction: bit-identical to the host evaluation.
 __device__ __forceinline__ float sellmeier_dev(float L, float T) {
     const float A = 4.502483f, B = 0.007294f, C = 0.185087f, D = -0.02357f;

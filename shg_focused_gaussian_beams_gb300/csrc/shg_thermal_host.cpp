@@ -3,6 +3,7 @@
 // reference's float rounding (Tfield.h:118-125).
 #include "shg_thermal_host.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <cstdlib>
@@ -138,7 +139,7 @@ int ThermalSolve::create(const shg_config &cfg) {
     TH_CUDA(cudaMalloc(&dkint_, nn * sizeof(float)));
     TH_CUDA(cudaMalloc(&f_, 6 * nn * sizeof(float2)));
     TH_CUDA(cudaMalloc(&stepc_, (size_t)nz_ * sizeof(float4)));
-    TH_CUDA(cudaMalloc(&acc_, 8 * sizeof(double)));  // [0..3] power sums, [4] list entry, [5] residual
+    TH_CUDA(cudaMalloc(&acc_, 8 * sizeof(double)));  // [0..3] power sums, [4] list entry, [5..6] residual sums
     TH_CUDA(cudaMalloc(&d_desc_, sizeof(InstDesc)));
     TH_CUDA(cudaMemset(qk_, 0, tsize_ * sizeof(float)));
     TH_CUDA(cudaMemset(acc_, 0, 8 * sizeof(double)));
@@ -176,6 +177,24 @@ int ThermalSolve::sweeps(float t_inf, int n) {
 // Solver.h:302-324: the residual is checked after the first sweep and then after every
 // 5000th; the loop stops when it is below 5e-4/TSIZE or equal to the previous check.
 int ThermalSolve::jacobi(float t_inf, int *counter) {
+    if (rel_tol_ > 0) {
+        // relative residual of one sweep, every check_every sweeps
+        int c = 0;
+        double sums[2];
+        for (;;) {
+            const int n = std::min(check_every_ - 1, max_sweeps_ - 1 - c);
+            if (n > 0) TH_TRY(sweeps(t_inf, n));
+            TH_TRY(sweeps(t_inf, 1));
+            c += n + 1;
+            TH_CUDA(launch_sq_sums(T_cur(), T_prev(), tsize_, scratch_sum_, st_));
+            TH_CUDA(cudaMemcpyAsync(sums, scratch_sum_, sizeof(sums), cudaMemcpyDeviceToHost, st_));
+            TH_CUDA(cudaStreamSynchronize(st_));
+            last_rel_ = sums[1] > 0 ? std::sqrt(sums[0] / sums[1]) : 0.0;
+            if (last_rel_ < rel_tol_ || c >= max_sweeps_) break;
+        }
+        *counter = c;
+        return SHG_OK;
+    }
     const float tol = (float)(5e-4 / (double)(unsigned)tsize_);
     float rs = 1.0f, aux = -1.0f;
     unsigned c = 0;

@@ -36,7 +36,16 @@ class ThermalSolve {
     bool has_result() const { return have_result_; }
 
     // Components (device buffers owned here).
-    int jacobi(float t_inf, int *counter);   // one Jacobi solve with the reference's stop rule
+    int jacobi(float t_inf, int *counter);   // one Jacobi solve with the configured stop rule
+    // Stop rule: rel_tol <= 0 (default) the reference's (Solver.h:302-324); otherwise stop
+    // once ||T_k+1 - T_k|| / ||T_k+1|| < rel_tol, checked every check_every sweeps, at most
+    // max_sweeps sweeps per solve.
+    void set_stop_rule(double rel_tol, int check_every, int max_sweeps) {
+        rel_tol_ = rel_tol;
+        check_every_ = check_every < 1 ? 1 : check_every;
+        max_sweeps_ = max_sweeps < 1 ? 1 : max_sweeps;
+    }
+    double last_residual() const { return last_rel_; }
     int sweeps(float t_inf, int n);          // n plain sweeps
     int cwes(float power, float waist, float focal);  // one thermal CWES from the current T
 
@@ -79,6 +88,8 @@ class ThermalSolve {
     bool have_result_ = false;
     int sh_seed_ = -1;
     float2 *slices_ = nullptr;
+    double rel_tol_ = 0.0, last_rel_ = -1.0;
+    int check_every_ = 100, max_sweeps_ = 1000000;
 };
 
 }  // namespace shg

@@ -146,6 +146,16 @@ class Solver:
         check(lib().shg_get_temperature(self._h, _pf(T)), "shg_get_temperature")
         return T
 
+    def set_jacobi_rule(self, rel_tol=0.0, check_every=100, max_sweeps=1000000):
+        """rel_tol <= 0: the reference's stop rule; else ||dT||/||T|| < rel_tol."""
+        check(lib().shg_set_jacobi_rule(self._h, float(rel_tol), int(check_every), int(max_sweeps)),
+              "shg_set_jacobi_rule")
+
+    def jacobi_residual(self) -> float:
+        r = C.c_double()
+        check(lib().shg_get_jacobi_residual(self._h, C.byref(r)), "shg_get_jacobi_residual")
+        return r.value
+
     def jacobi_counts(self):
         c = (C.c_int * 5)()
         check(lib().shg_get_jacobi_counts(self._h, c), "shg_get_jacobi_counts")

@@ -108,3 +108,22 @@ def test_thermal_run_64_oven_vs_oracle():
     po, so = s.fields()
     assert rel_l2(so, ref["sh"]) < FIELD_RTOL
     assert np.max(np.abs(s.temperature() - ref["T"])) < 1e-4
+
+
+def test_relative_residual_stop_rule():
+    """The THERMAL workload's relative-residual rule: each Jacobi solve stops once one
+    sweep changes T by less than 1e-6 relative; the counts differ from the reference rule's
+    and the fields agree to the convergence level of the two rules (Jacobi converges slowly,
+    so a 1e-6 relative step leaves a residual error of a fraction of a kelvin)."""
+    inst = W.plain_instance(64, 60, 25.0, 2.84, 51.0)
+    a = S.Solver(crystal=W.CRYSTAL_QPM50, nx=64, ny=64, nz=60, lx=inst.lx, ly=inst.ly, thermal=True, bc=1)
+    a.run(25.0, inst.waist, FOCAL, 51.0, 25.0, 51.0, 51.0)
+    b = S.Solver(crystal=W.CRYSTAL_QPM50, nx=64, ny=64, nz=60, lx=inst.lx, ly=inst.ly, thermal=True, bc=1)
+    b.set_jacobi_rule(1e-6, check_every=50)
+    b.run(25.0, inst.waist, FOCAL, 51.0, 25.0, 51.0, 51.0)
+    assert 0 <= b.jacobi_residual() < 1e-6
+    cb = b.jacobi_counts()
+    assert cb[0] >= 50 and all(c % 50 == 0 for c in cb if c > 0)
+    assert cb != a.jacobi_counts()
+    assert np.max(np.abs(b.temperature() - a.temperature())) < 0.25
+    assert abs(b.efficiency() - a.efficiency()) / a.efficiency() < 0.1
