@@ -164,8 +164,9 @@ int shg_batch_launch_count(shg_batch *b, int *launches);
 /* Schedule autotuner. Each grid-size class of the batch marches either as streaming
  * row/column launches or as one persistent resident launch (a thread-block cluster per
  * solve, fields in shared memory) in one of several (cluster size, CTAs per SM) variants.
+ * Resident variants also differ in the line-FFT split (n = 64: 8 x 8 or 16 x 4 points).
  * Unless the environment variable SHG_MARCH is "streaming", "resident" (default variants)
- * or lists a schedule per grid ("64:1/1,128:4/2,256:16/2", "64:streaming"), the first run
+ * or lists a schedule per grid ("64:1/1,128:4/2,256:16/2", "64:1/1/4", "64:streaming"), the first run
  * times every candidate on the class's own solves and keeps the fastest (cached per
  * device and class shape for the process). shg_batch_autotune does that now, outside any
  * stream capture; shg_batch_schedule writes the choices and trial times as text. */
@@ -175,6 +176,9 @@ int shg_batch_autotune(shg_batch *b, void *stream);
  * (1, 1); n = 64 (1, 1), (1, 2), (2, 2), (2, 4); n = 128 (2, 1), (4, 1), (4, 2); n = 256
  * (8, 1), (16, 1), (16, 2)). SHG_ERR_UNSUPPORTED if the variant does not exist or fit. */
 int shg_batch_set_schedule(shg_batch *b, int n, int resident, int cluster_size, int ctas_per_sm);
+/* Same for a resident variant with a given line-FFT split: threads_per_line G, each thread
+ * holding N/G points (n = 64: G = 8 or 4; other grids: their one split). */
+int shg_batch_set_schedule_split(shg_batch *b, int n, int cluster_size, int ctas_per_sm, int threads_per_line);
 int shg_batch_schedule(shg_batch *b, char *buf, int len);
 /* Diagnostic: one concurrent run without a graph, with events around each grid-size class
  * launched on its own stream as a run launches them; start_end[2k], start_end[2k+1] = start

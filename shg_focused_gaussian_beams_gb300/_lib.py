@@ -68,6 +68,7 @@ SIGNATURES = {
     "shg_batch_autotune": (_i, [_vp, _vp]),
     "shg_batch_schedule": (_i, [_vp, C.c_char_p, _i]),
     "shg_batch_set_schedule": (_i, [_vp, _i, _i, _i, _i]),
+    "shg_batch_set_schedule_split": (_i, [_vp, _i, _i, _i, _i]),
     "shg_batch_timeline": (_i, [_vp, _pd, _i, _pi, _vp]),
     "shg_batch_io_bytes": (_i, [_vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "shg_dft2d_device": (_i, [_i, _i, _vp, _vp, _vp]),

@@ -270,15 +270,15 @@ class Batch {
                 pos = end + 1;
                 if (item.compare(0, key.size(), key) != 0) continue;
                 const std::string v = item.substr(key.size());
-                int cs = 0, mb = 0;
+                int cs = 0, mb = 0, g = 0;
                 if (v == "streaming") {
                     c.resident = false;
                     c.tuned = true;
-                } else if (std::sscanf(v.c_str(), "%d/%d", &cs, &mb) == 2) {
+                } else if (std::sscanf(v.c_str(), "%d/%d/%d", &cs, &mb, &g) >= 2) {
                     ResidentVariant vs[8];
                     const int nv = resident_variants(c.n, vs, 8);
-                    for (int i = 0; i < nv; ++i)
-                        if (vs[i].cs == cs && vs[i].minb == mb) {
+                    for (int i = nv - 1; i >= 0; --i)
+                        if (vs[i].cs == cs && vs[i].minb == mb && (g == 0 || vs[i].g == g)) {
                             c.resident = true;
                             c.var = vs[i];
                             c.tuned = true;
@@ -440,7 +440,7 @@ class Batch {
                 ResidentVariant v;
                 int clusters;
             };
-            std::vector<Cand> cands{{false, {0, 0}, 0}};
+            std::vector<Cand> cands{{false, {0, 0, 0}, 0}};
             ResidentVariant vs[8];
             const int nv = resident_variants(c.n, vs, 8);
             for (int i = 0; i < nv; ++i) {
@@ -500,7 +500,7 @@ class Batch {
 
     // Fixes the schedule of grid-size class n: streaming (resident = 0) or the resident
     // variant (cs, minb), which must be one of resident_variants(n) and fit on the device.
-    int set_schedule(int n, int resident, int cs, int minb) {
+    int set_schedule(int n, int resident, int cs, int minb, int g = 0) {
         for (auto &c : classes_) {
             if (c.n != n) continue;
             if (!resident) {
@@ -508,16 +508,17 @@ class Batch {
             } else {
                 ResidentVariant vs[8];
                 const int nv = resident_variants(n, vs, 8);
-                bool ok = false;
-                for (int i = 0; i < nv; ++i) ok |= vs[i].cs == cs && vs[i].minb == minb;
+                int hit = -1;
+                for (int i = nv - 1; i >= 0; --i)
+                    if (vs[i].cs == cs && vs[i].minb == minb && (g == 0 || vs[i].g == g)) hit = i;
                 int mc = 0;
-                if (!ok || prepare_resident(n, ResidentVariant{cs, minb}, &mc) != cudaSuccess || mc < 1) {
+                if (hit < 0 || prepare_resident(n, vs[hit], &mc) != cudaSuccess || mc < 1) {
                     cudaGetLastError();
                     set_error("set_schedule: no such resident variant for this grid, or it does not fit");
                     return SHG_ERR_UNSUPPORTED;
                 }
                 c.resident = true;
-                c.var = ResidentVariant{cs, minb};
+                c.var = vs[hit];
                 c.max_clusters = mc;
             }
             c.tuned = true;
@@ -569,7 +570,8 @@ class Batch {
         for (const auto &c : classes_) {
             out += "n=" + std::to_string(c.n) + " solves=" + std::to_string(c.count) + ": ";
             out += !c.tuned ? "untuned" : c.resident ? "resident cs=" + std::to_string(c.var.cs) +
-                                                             " minb=" + std::to_string(c.var.minb)
+                                                             " minb=" + std::to_string(c.var.minb) +
+                                                             " g=" + std::to_string(c.var.g)
                                                        : std::string("streaming");
             if (!c.trials.empty()) {
                 out += " [";
@@ -577,7 +579,8 @@ class Batch {
                     const auto &t = c.trials[i];
                     char buf[96];
                     std::snprintf(buf, sizeof(buf), "%s%s %.3f", i ? ", " : "",
-                                  t.resident ? ("cs" + std::to_string(t.v.cs) + "/" + std::to_string(t.v.minb)).c_str()
+                                  t.resident ? ("cs" + std::to_string(t.v.cs) + "/" + std::to_string(t.v.minb) + "/" +
+                                                std::to_string(t.v.g)).c_str()
                                              : "streaming",
                                   t.ms);
                     out += buf;
@@ -634,7 +637,7 @@ class Batch {
         std::vector<int> steps;  // descending
         bool tuned = false;      // schedule chosen (by SHG_MARCH or the autotuner)
         bool resident = true;    // resident march (else streaming row / column launches)
-        ResidentVariant var{1, 1};
+        ResidentVariant var{1, 1, 0};
         int max_clusters = 0;    // resident march: clusters resident at once
         double pt_steps = 0;     // sum of n*n*nsteps
         std::vector<Trial> trials;
@@ -1491,6 +1494,14 @@ int shg_batch_set_schedule(shg_batch *b, int n, int resident, int cluster_size, 
         return SHG_ERR_INVALID;
     }
     return b->batch.set_schedule(n, resident, cluster_size, ctas_per_sm);
+}
+
+int shg_batch_set_schedule_split(shg_batch *b, int n, int cluster_size, int ctas_per_sm, int threads_per_line) {
+    if (!b) {
+        set_error("null argument");
+        return SHG_ERR_INVALID;
+    }
+    return b->batch.set_schedule(n, 1, cluster_size, ctas_per_sm, threads_per_line);
 }
 
 int shg_batch_schedule(shg_batch *b, char *buf, int len) {

@@ -21,7 +21,7 @@ const float2 *twiddle_symbol_address_resident256();
 
 // shg_march_v1.cu (resident march): variants (cluster size, CTAs per SM) per grid size
 struct ResidentVariant {
-    int cs, minb;
+    int cs, minb, g;  // cluster size, CTAs per SM, threads per line (FFT split N = (N/g) x g)
 };
 int resident_variants(int n, ResidentVariant *out, int max_out);
 ResidentVariant resident_default(int n);

@@ -21,34 +21,35 @@
 // left. No cluster waits on another, so a cluster that starts late only finds fewer solves.
 //
 // The kernel template lives in shg_resident.cuh and is instantiated per grid size in
-// shg_resident_{64,128,256}.cu; this file lists the variants (cluster size CS and CTAs
-// per SM MINB) that the batch schedule's autotuner times, and dispatches to them.
+// shg_resident_{64,128,256}.cu; this file lists the variants (cluster size CS, CTAs per SM
+// MINB, and the line-FFT split G: E = N/G point register DFTs, then G-point ones) that the
+// batch schedule's autotuner times, and dispatches to them.
 #include <cuda_runtime.h>
 
 #include "shg_internal.h"
 
 namespace shg {
 
-cudaError_t prepare_resident_small(int n, int cs, int minb, int *max_clusters);
-cudaError_t launch_resident_small(int n, int cs, int minb, const InstDesc *inst, const int *list, int njobs,
+cudaError_t prepare_resident_small(int n, int cs, int minb, int g, int *max_clusters);
+cudaError_t launch_resident_small(int n, int cs, int minb, int g, const InstDesc *inst, const int *list, int njobs,
                                   int *counter, int max_clusters, cudaStream_t st);
-cudaError_t prepare_resident_128(int cs, int minb, int *max_clusters);
-cudaError_t launch_resident_128(int cs, int minb, const InstDesc *inst, const int *list, int njobs, int *counter,
+cudaError_t prepare_resident_128(int cs, int minb, int g, int *max_clusters);
+cudaError_t launch_resident_128(int cs, int minb, int g, const InstDesc *inst, const int *list, int njobs, int *counter,
                                 int max_clusters, cudaStream_t st);
-cudaError_t prepare_resident_256(int cs, int minb, int *max_clusters);
-cudaError_t launch_resident_256(int cs, int minb, const InstDesc *inst, const int *list, int njobs, int *counter,
+cudaError_t prepare_resident_256(int cs, int minb, int g, int *max_clusters);
+cudaError_t launch_resident_256(int cs, int minb, int g, const InstDesc *inst, const int *list, int njobs, int *counter,
                                 int max_clusters, cudaStream_t st);
 
 int resident_variants(int n, ResidentVariant *out, int max_out) {
-    static const ResidentVariant v16[] = {{1, 1}};
-    static const ResidentVariant v64[] = {{1, 1}, {1, 2}, {2, 2}, {2, 4}};
-    static const ResidentVariant v128[] = {{2, 1}, {4, 1}, {4, 2}};
-    static const ResidentVariant v256[] = {{8, 1}, {16, 1}, {16, 2}};
+    static const ResidentVariant v16[] = {{1, 1, 4}};
+    static const ResidentVariant v64[] = {{1, 1, 8}, {1, 2, 8}, {2, 2, 8}, {2, 4, 8}, {1, 1, 4}, {1, 2, 4}};
+    static const ResidentVariant v128[] = {{2, 1, 8}, {4, 1, 8}, {4, 2, 8}};
+    static const ResidentVariant v256[] = {{8, 1, 16}, {16, 1, 16}, {16, 2, 16}};
     const ResidentVariant *v = nullptr;
     int c = 0;
     switch (n) {
         case 16: case 32: v = v16; c = 1; break;
-        case 64: v = v64; c = 4; break;
+        case 64: v = v64; c = 6; break;
         case 128: v = v128; c = 3; break;
         case 256: v = v256; c = 3; break;
         default: return 0;
@@ -58,16 +59,16 @@ int resident_variants(int n, ResidentVariant *out, int max_out) {
 }
 
 ResidentVariant resident_default(int n) {
-    ResidentVariant v{1, 1};
+    ResidentVariant v{1, 1, 0};
     resident_variants(n, &v, 1);
     return v;
 }
 
 cudaError_t prepare_resident(int n, ResidentVariant v, int *max_clusters) {
     switch (n) {
-        case 16: case 32: case 64: return prepare_resident_small(n, v.cs, v.minb, max_clusters);
-        case 128: return prepare_resident_128(v.cs, v.minb, max_clusters);
-        case 256: return prepare_resident_256(v.cs, v.minb, max_clusters);
+        case 16: case 32: case 64: return prepare_resident_small(n, v.cs, v.minb, v.g, max_clusters);
+        case 128: return prepare_resident_128(v.cs, v.minb, v.g, max_clusters);
+        case 256: return prepare_resident_256(v.cs, v.minb, v.g, max_clusters);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -76,9 +77,9 @@ cudaError_t launch_resident(int n, ResidentVariant v, const InstDesc *inst, cons
                             int max_clusters, cudaStream_t st) {
     switch (n) {
         case 16: case 32: case 64:
-            return launch_resident_small(n, v.cs, v.minb, inst, list, njobs, counter, max_clusters, st);
-        case 128: return launch_resident_128(v.cs, v.minb, inst, list, njobs, counter, max_clusters, st);
-        case 256: return launch_resident_256(v.cs, v.minb, inst, list, njobs, counter, max_clusters, st);
+            return launch_resident_small(n, v.cs, v.minb, v.g, inst, list, njobs, counter, max_clusters, st);
+        case 128: return launch_resident_128(v.cs, v.minb, v.g, inst, list, njobs, counter, max_clusters, st);
+        case 256: return launch_resident_256(v.cs, v.minb, v.g, inst, list, njobs, counter, max_clusters, st);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -14,10 +14,10 @@ namespace shg {
 
 // Shape of one resident variant: CS CTAs per cluster, MINB CTAs per SM requested from the
 // register allocator.
-template <int N, int CS_, int MINB_>
+template <int N, int CS_, int MINB_, int G_ = LineShape<N>::G>
 struct ResShape {
     static constexpr int CS = CS_, MINB = MINB_;
-    static constexpr int G = LineShape<N>::G, E = N / G;
+    static constexpr int G = G_, E = N / G;   // line FFT split: E-point register DFTs, then G-point
     static constexpr int R = N / CS;             // rows (and columns) per CTA
     static constexpr int THREADS = R * G;
     static constexpr int SC_ROW = LineScratch<N, G>::SIZE;
@@ -48,10 +48,10 @@ __device__ __forceinline__ void block_add_double_res(double v, double *dst) {
     }
 }
 
-template <int N, int CS_, int MINB_>
-__global__ void __launch_bounds__(ResShape<N, CS_, MINB_>::THREADS, MINB_)
+template <int N, int CS_, int MINB_, int G_>
+__global__ void __launch_bounds__(ResShape<N, CS_, MINB_, G_>::THREADS, MINB_)
     k_march_resident(const InstDesc *__restrict__ inst, const int *__restrict__ list, int njobs, int *counter) {
-    using Sh = ResShape<N, CS_, MINB_>;
+    using Sh = ResShape<N, CS_, MINB_, G_>;
     constexpr int CS = Sh::CS, G = Sh::G, E = Sh::E, R = Sh::R, FIELD = Sh::FIELD, SC_ROW = Sh::SC_ROW;
     extern __shared__ float2 smem[];
     float2 *sP = smem, *sS = smem + FIELD, *scr = smem + 2 * FIELD;
@@ -192,9 +192,9 @@ __global__ void __launch_bounds__(ResShape<N, CS_, MINB_>::THREADS, MINB_)
     }
 }
 
-template <int N, int CS, int MINB>
+template <int N, int CS, int MINB, int G>
 static cudaLaunchConfig_t resident_config(cudaLaunchAttribute *attr, cudaStream_t st) {
-    using Sh = ResShape<N, CS, MINB>;
+    using Sh = ResShape<N, CS, MINB, G>;
     cudaLaunchConfig_t cfg = {};
     cfg.blockDim = dim3(Sh::THREADS, 1, 1);
     cfg.dynamicSmemBytes = Sh::SMEM;
@@ -210,10 +210,10 @@ static cudaLaunchConfig_t resident_config(cudaLaunchAttribute *attr, cudaStream_
 
 // Once per device, outside any stream capture: shared-memory limit, cluster size above the
 // portable 8 where asked, and the number of clusters that fit at once (0: does not fit).
-template <int N, int CS, int MINB>
+template <int N, int CS, int MINB, int G>
 cudaError_t prepare_resident_t(int *max_clusters) {
-    using Sh = ResShape<N, CS, MINB>;
-    auto k = k_march_resident<N, CS, MINB>;
+    using Sh = ResShape<N, CS, MINB, G>;
+    auto k = k_march_resident<N, CS, MINB, G>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Sh::SMEM);
     if (e != cudaSuccess) return e;
     if (CS > 8) {
@@ -221,27 +221,27 @@ cudaError_t prepare_resident_t(int *max_clusters) {
         if (e != cudaSuccess) return e;
     }
     cudaLaunchAttribute attr[1];
-    cudaLaunchConfig_t cfg = resident_config<N, CS, MINB>(attr, nullptr);
+    cudaLaunchConfig_t cfg = resident_config<N, CS, MINB, G>(attr, nullptr);
     cfg.gridDim = dim3(Sh::CS, 1, 1);
     return cudaOccupancyMaxActiveClusters(max_clusters, k, &cfg);
 }
 
-template <int N, int CS, int MINB>
+template <int N, int CS, int MINB, int G>
 cudaError_t launch_resident_t(const InstDesc *inst, const int *list, int njobs, int *counter, int max_clusters,
                               cudaStream_t st) {
     cudaLaunchAttribute attr[1];
-    cudaLaunchConfig_t cfg = resident_config<N, CS, MINB>(attr, st);
+    cudaLaunchConfig_t cfg = resident_config<N, CS, MINB, G>(attr, st);
     int clusters = max_clusters;
     if (clusters > njobs) clusters = njobs;
     if (clusters < 1) clusters = 1;
     cfg.gridDim = dim3(clusters * CS, 1, 1);
-    return cudaLaunchKernelEx(&cfg, k_march_resident<N, CS, MINB>, inst, list, njobs, counter);
+    return cudaLaunchKernelEx(&cfg, k_march_resident<N, CS, MINB, G>, inst, list, njobs, counter);
 }
 
-// Variants compiled for grid n (its translation unit), as (CS, MINB) pairs.
-#define SHG_RESIDENT_INSTANTIATE(N, CS, MINB)                                                              \
-    template cudaError_t prepare_resident_t<N, CS, MINB>(int *);                                         \
-    template cudaError_t launch_resident_t<N, CS, MINB>(const InstDesc *, const int *, int, int *, int,  \
-                                                        cudaStream_t);
+// Variants compiled for grid n (its translation unit), as (CS, MINB, G) triples.
+#define SHG_RESIDENT_INSTANTIATE(N, CS, MINB, G)                                                              \
+    template cudaError_t prepare_resident_t<N, CS, MINB, G>(int *);                                         \
+    template cudaError_t launch_resident_t<N, CS, MINB, G>(const InstDesc *, const int *, int, int *, int,  \
+                                                           cudaStream_t);
 
 }  // namespace shg

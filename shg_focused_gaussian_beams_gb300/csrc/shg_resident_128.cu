@@ -9,22 +9,24 @@ const float2 *twiddle_symbol_address_resident128() {
     return static_cast<const float2 *>(p);
 }
 
-SHG_RESIDENT_INSTANTIATE(128, 2, 1)
-SHG_RESIDENT_INSTANTIATE(128, 4, 1)
-SHG_RESIDENT_INSTANTIATE(128, 4, 2)
+SHG_RESIDENT_INSTANTIATE(128, 2, 1, 8)
+SHG_RESIDENT_INSTANTIATE(128, 4, 1, 8)
+SHG_RESIDENT_INSTANTIATE(128, 4, 2, 8)
 
-cudaError_t prepare_resident_128(int cs, int minb, int *m) {
-    if (cs == 2 && minb == 1) return prepare_resident_t<128, 2, 1>(m);
-    if (cs == 4 && minb == 1) return prepare_resident_t<128, 4, 1>(m);
-    if (cs == 4 && minb == 2) return prepare_resident_t<128, 4, 2>(m);
+cudaError_t prepare_resident_128(int cs, int minb, int g, int *m) {
+    if (g != 8) return cudaErrorInvalidValue;
+    if (cs == 2 && minb == 1) return prepare_resident_t<128, 2, 1, 8>(m);
+    if (cs == 4 && minb == 1) return prepare_resident_t<128, 4, 1, 8>(m);
+    if (cs == 4 && minb == 2) return prepare_resident_t<128, 4, 2, 8>(m);
     return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_resident_128(int cs, int minb, const InstDesc *inst, const int *list, int njobs, int *counter,
+cudaError_t launch_resident_128(int cs, int minb, int g, const InstDesc *inst, const int *list, int njobs, int *counter,
                                 int max_clusters, cudaStream_t st) {
-    if (cs == 2 && minb == 1) return launch_resident_t<128, 2, 1>(inst, list, njobs, counter, max_clusters, st);
-    if (cs == 4 && minb == 1) return launch_resident_t<128, 4, 1>(inst, list, njobs, counter, max_clusters, st);
-    if (cs == 4 && minb == 2) return launch_resident_t<128, 4, 2>(inst, list, njobs, counter, max_clusters, st);
+    if (g != 8) return cudaErrorInvalidValue;
+    if (cs == 2 && minb == 1) return launch_resident_t<128, 2, 1, 8>(inst, list, njobs, counter, max_clusters, st);
+    if (cs == 4 && minb == 1) return launch_resident_t<128, 4, 1, 8>(inst, list, njobs, counter, max_clusters, st);
+    if (cs == 4 && minb == 2) return launch_resident_t<128, 4, 2, 8>(inst, list, njobs, counter, max_clusters, st);
     return cudaErrorInvalidValue;
 }
 

@@ -9,22 +9,24 @@ const float2 *twiddle_symbol_address_resident256() {
     return static_cast<const float2 *>(p);
 }
 
-SHG_RESIDENT_INSTANTIATE(256, 8, 1)
-SHG_RESIDENT_INSTANTIATE(256, 16, 1)
-SHG_RESIDENT_INSTANTIATE(256, 16, 2)
+SHG_RESIDENT_INSTANTIATE(256, 8, 1, 16)
+SHG_RESIDENT_INSTANTIATE(256, 16, 1, 16)
+SHG_RESIDENT_INSTANTIATE(256, 16, 2, 16)
 
-cudaError_t prepare_resident_256(int cs, int minb, int *m) {
-    if (cs == 8 && minb == 1) return prepare_resident_t<256, 8, 1>(m);
-    if (cs == 16 && minb == 1) return prepare_resident_t<256, 16, 1>(m);
-    if (cs == 16 && minb == 2) return prepare_resident_t<256, 16, 2>(m);
+cudaError_t prepare_resident_256(int cs, int minb, int g, int *m) {
+    if (g != 16) return cudaErrorInvalidValue;
+    if (cs == 8 && minb == 1) return prepare_resident_t<256, 8, 1, 16>(m);
+    if (cs == 16 && minb == 1) return prepare_resident_t<256, 16, 1, 16>(m);
+    if (cs == 16 && minb == 2) return prepare_resident_t<256, 16, 2, 16>(m);
     return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_resident_256(int cs, int minb, const InstDesc *inst, const int *list, int njobs, int *counter,
+cudaError_t launch_resident_256(int cs, int minb, int g, const InstDesc *inst, const int *list, int njobs, int *counter,
                                 int max_clusters, cudaStream_t st) {
-    if (cs == 8 && minb == 1) return launch_resident_t<256, 8, 1>(inst, list, njobs, counter, max_clusters, st);
-    if (cs == 16 && minb == 1) return launch_resident_t<256, 16, 1>(inst, list, njobs, counter, max_clusters, st);
-    if (cs == 16 && minb == 2) return launch_resident_t<256, 16, 2>(inst, list, njobs, counter, max_clusters, st);
+    if (g != 16) return cudaErrorInvalidValue;
+    if (cs == 8 && minb == 1) return launch_resident_t<256, 8, 1, 16>(inst, list, njobs, counter, max_clusters, st);
+    if (cs == 16 && minb == 1) return launch_resident_t<256, 16, 1, 16>(inst, list, njobs, counter, max_clusters, st);
+    if (cs == 16 && minb == 2) return launch_resident_t<256, 16, 2, 16>(inst, list, njobs, counter, max_clusters, st);
     return cudaErrorInvalidValue;
 }
 

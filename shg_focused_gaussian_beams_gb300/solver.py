@@ -255,8 +255,13 @@ class Sweep:
         """Time the schedules of every grid-size class now (outside any capture)."""
         check(lib().shg_batch_autotune(self._b, stream), "shg_batch_autotune")
 
-    def set_schedule(self, n, resident=True, cluster_size=1, ctas_per_sm=1):
-        """Fix the schedule of the grid-n class (streaming, or a resident variant)."""
+    def set_schedule(self, n, resident=True, cluster_size=1, ctas_per_sm=1, threads_per_line=None):
+        """Fix the schedule of the grid-n class (streaming, or a resident variant, optionally
+        with its line-FFT split)."""
+        if resident and threads_per_line:
+            check(lib().shg_batch_set_schedule_split(self._b, int(n), int(cluster_size), int(ctas_per_sm),
+                                                     int(threads_per_line)), "shg_batch_set_schedule_split")
+            return
         check(lib().shg_batch_set_schedule(self._b, int(n), int(bool(resident)), int(cluster_size),
                                            int(ctas_per_sm)), "shg_batch_set_schedule")
 
