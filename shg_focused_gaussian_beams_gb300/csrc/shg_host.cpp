@@ -487,6 +487,7 @@ class Batch {
             std::lock_guard<std::mutex> lock(mu);
             cache[key] = {c.resident, c.var};
         }
+        if (rc == SHG_OK) rc = tune_mix(st, a, b);
         cudaEventDestroy(a);
         cudaEventDestroy(b);
         if (rc && rc != SHG_ERR_CUDA) return rc;
@@ -495,6 +496,101 @@ class Batch {
             return rc;
         }
         invalidate_graph();
+        return SHG_OK;
+    }
+
+    // Second stage: the classes share the GPU in a run (one stream each), so the fastest
+    // schedule of a class alone is not always the fastest beside the others. The largest
+    // grid keeps its choice; for each other class the two fastest schedules alone are tried,
+    // timing the whole concurrent run of every combination as a captured graph (second of
+    // two launches). Cached per device and batch shape.
+    int tune_mix(cudaStream_t st, cudaEvent_t a, cudaEvent_t b) {
+        const int nc = (int)classes_.size();
+        mix_.clear();
+        if (nc < 2) return SHG_OK;
+        std::vector<int> order(nc);
+        for (int i = 0; i < nc; ++i) order[i] = i;
+        std::sort(order.begin(), order.end(), [&](int x, int y) { return classes_[x].n > classes_[y].n; });
+        std::string key = std::to_string(cr_.device);
+        for (int ci : order) {
+            char buf[96];
+            std::snprintf(buf, sizeof(buf), "|%d:%d:%.17g", classes_[ci].n, classes_[ci].count, classes_[ci].pt_steps);
+            key += buf;
+        }
+        struct Pick {
+            bool resident;
+            ResidentVariant v;
+        };
+        static std::mutex mu;
+        static std::map<std::string, std::vector<Pick>> cache;
+        auto apply = [&](int ci, const Pick &p) -> int {
+            Class &c = classes_[ci];
+            c.resident = p.resident;
+            c.var = p.v;
+            if (c.resident && prepare_resident(c.n, c.var, &c.max_clusters) != cudaSuccess) {
+                cudaGetLastError();
+                return SHG_ERR_CUDA;
+            }
+            return SHG_OK;
+        };
+        {
+            std::lock_guard<std::mutex> lock(mu);
+            auto it = cache.find(key);
+            if (it != cache.end()) {
+                for (int oi = 0; oi < nc; ++oi) SHG_TRY_INT(apply(order[oi], it->second[oi]));
+                return SHG_OK;
+            }
+        }
+        std::vector<std::vector<Pick>> opts(nc);
+        opts[0].push_back({classes_[order[0]].resident, classes_[order[0]].var});
+        int ncomb = 1;
+        for (int oi = 1; oi < nc; ++oi) {
+            auto t = classes_[order[oi]].trials;
+            if (t.empty()) return SHG_OK;  // schedule fixed by the caller: keep it
+            std::sort(t.begin(), t.end(), [](const Trial &x, const Trial &y) { return x.ms < y.ms; });
+            for (int k = 0; k < (int)t.size() && k < 2; ++k) opts[oi].push_back({t[k].resident, t[k].v});
+            ncomb *= (int)opts[oi].size();
+        }
+        float best = 1e30f;
+        int bi = 0;
+        for (int comb = 0; comb < ncomb; ++comb) {
+            int r = comb;
+            std::string label;
+            for (int oi = 0; oi < nc; ++oi) {
+                const int k = r % (int)opts[oi].size();
+                r /= (int)opts[oi].size();
+                const Pick &p = opts[oi][k];
+                SHG_TRY_INT(apply(order[oi], p));
+                label += (oi ? "," : "") + std::to_string(classes_[order[oi]].n) + ":" +
+                         (p.resident ? std::to_string(p.v.cs) + "/" + std::to_string(p.v.minb) + "/" +
+                                           std::to_string(p.v.g)
+                                     : std::string("streaming"));
+            }
+            // time the combination as runs execute it: a captured graph, second launch counted
+            float ms = 0.f;
+            invalidate_graph();
+            SHG_TRY_INT(run_async(st, true));
+            if (cudaEventRecord(a, st) != cudaSuccess) return SHG_ERR_CUDA;
+            SHG_TRY_INT(run_async(st, true));
+            if (cudaEventRecord(b, st) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess ||
+                cudaEventElapsedTime(&ms, a, b) != cudaSuccess)
+                return SHG_ERR_CUDA;
+            mix_.push_back({label, ms});
+            if (ms < best) {
+                best = ms;
+                bi = comb;
+            }
+        }
+        std::vector<Pick> chosen(nc);
+        int r = bi;
+        for (int oi = 0; oi < nc; ++oi) {
+            const int k = r % (int)opts[oi].size();
+            r /= (int)opts[oi].size();
+            chosen[oi] = opts[oi][k];
+            SHG_TRY_INT(apply(order[oi], chosen[oi]));
+        }
+        std::lock_guard<std::mutex> lock(mu);
+        cache[key] = chosen;
         return SHG_OK;
     }
 
@@ -586,6 +682,15 @@ class Batch {
                     out += buf;
                 }
                 out += " ms]";
+            }
+            out += "\n";
+        }
+        if (!mix_.empty()) {
+            out += "concurrent run:";
+            for (const auto &m : mix_) {
+                char buf[160];
+                std::snprintf(buf, sizeof(buf), " [%s %.3f ms]", m.first.c_str(), m.second);
+                out += buf;
             }
             out += "\n";
         }
@@ -833,6 +938,7 @@ class Batch {
     cudaGraphExec_t graph_exec_ = nullptr;
     cudaStream_t capture_stream_ = nullptr;
     int *d_counters_ = nullptr;
+    std::vector<std::pair<std::string, float>> mix_;  // concurrent-run trials of the autotuner
     std::vector<cudaStream_t> side_streams_;
     std::vector<cudaEvent_t> side_events_;
     cudaEvent_t fork_event_ = nullptr;
