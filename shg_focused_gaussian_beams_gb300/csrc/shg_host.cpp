@@ -500,10 +500,10 @@ class Batch {
     }
 
     // Second stage: the classes share the GPU in a run (one stream each), so the fastest
-    // schedule of a class alone is not always the fastest beside the others. The largest
-    // grid keeps its choice; for each other class the two fastest schedules alone are tried,
-    // timing the whole concurrent run of every combination as a captured graph (second of
-    // two launches). Cached per device and batch shape.
+    // schedule of a class alone is not always the fastest beside the others. For each class
+    // the two fastest schedules alone are tried, timing the whole concurrent run of every
+    // combination as a captured graph (second of two launches). Cached per device and batch
+    // shape.
     int tune_mix(cudaStream_t st, cudaEvent_t a, cudaEvent_t b) {
         const int nc = (int)classes_.size();
         mix_.clear();
@@ -542,9 +542,8 @@ class Batch {
             }
         }
         std::vector<std::vector<Pick>> opts(nc);
-        opts[0].push_back({classes_[order[0]].resident, classes_[order[0]].var});
         int ncomb = 1;
-        for (int oi = 1; oi < nc; ++oi) {
+        for (int oi = 0; oi < nc; ++oi) {
             auto t = classes_[order[oi]].trials;
             if (t.empty()) return SHG_OK;  // schedule fixed by the caller: keep it
             std::sort(t.begin(), t.end(), [](const Trial &x, const Trial &y) { return x.ms < y.ms; });
