@@ -275,8 +275,8 @@ class Batch {
                     c.resident = false;
                     c.tuned = true;
                 } else if (std::sscanf(v.c_str(), "%d/%d/%d", &cs, &mb, &g) >= 2) {
-                    ResidentVariant vs[8];
-                    const int nv = resident_variants(c.n, vs, 8);
+                    ResidentVariant vs[16];
+                    const int nv = resident_variants(c.n, vs, 16);
                     for (int i = nv - 1; i >= 0; --i)
                         if (vs[i].cs == cs && vs[i].minb == mb && (g == 0 || vs[i].g == g)) {
                             c.resident = true;
@@ -441,8 +441,8 @@ class Batch {
                 int clusters;
             };
             std::vector<Cand> cands{{false, {0, 0, 0}, 0}};
-            ResidentVariant vs[8];
-            const int nv = resident_variants(c.n, vs, 8);
+            ResidentVariant vs[16];
+            const int nv = resident_variants(c.n, vs, 16);
             for (int i = 0; i < nv; ++i) {
                 int mc = 0;
                 if (prepare_resident(c.n, vs[i], &mc) == cudaSuccess && mc > 0)
@@ -601,8 +601,8 @@ class Batch {
             if (!resident) {
                 c.resident = false;
             } else {
-                ResidentVariant vs[8];
-                const int nv = resident_variants(n, vs, 8);
+                ResidentVariant vs[16];
+                const int nv = resident_variants(n, vs, 16);
                 int hit = -1;
                 for (int i = nv - 1; i >= 0; --i)
                     if (vs[i].cs == cs && vs[i].minb == minb && (g == 0 || vs[i].g == g)) hit = i;

@@ -1,7 +1,8 @@
 // Resident z-march: every solve keeps both fields in shared memory for its whole march.
 //
-// A solve of N x N points is owned by a thread-block cluster of CS CTAs (variants: CS = 1
-// or 2 for N = 64, 2 or 4 for N = 128, 8 or 16 for N = 256); CTA r of the cluster holds rows
+// A solve of N x N points is owned by a thread-block cluster of CS CTAs (variants: CS = 1,
+// 2, 4 or 8 for N = 64, 2, 4, 8 or 16 for N = 128, 8 or 16 for N = 256; the large clusters
+// spread one solve over more SMs, which shortens a lone solve); CTA r of the cluster holds rows
 // [r*R, (r+1)*R), R = N / CS, of the pump and SH fields. Per SSFM step:
 //   row phase (local):   forward FFT along x finishing step s-1, RK4(z_{s-1}),
 //                        [capture at the top of slice nz-1], RK4(z_s), backward FFT;
@@ -42,15 +43,16 @@ cudaError_t launch_resident_256(int cs, int minb, int g, const InstDesc *inst, c
 
 int resident_variants(int n, ResidentVariant *out, int max_out) {
     static const ResidentVariant v16[] = {{1, 1, 4}};
-    static const ResidentVariant v64[] = {{1, 1, 8}, {1, 2, 8}, {2, 2, 8}, {2, 4, 8}, {1, 1, 4}, {1, 2, 4}};
-    static const ResidentVariant v128[] = {{2, 1, 8}, {4, 1, 8}, {4, 2, 8}};
+    static const ResidentVariant v64[] = {{1, 1, 8}, {1, 2, 8}, {2, 2, 8}, {2, 4, 8}, {1, 1, 4}, {1, 2, 4},
+                                          {4, 4, 8}, {8, 8, 8}};
+    static const ResidentVariant v128[] = {{2, 1, 8}, {4, 1, 8}, {4, 2, 8}, {8, 4, 8}, {16, 8, 8}};
     static const ResidentVariant v256[] = {{8, 1, 16}, {16, 1, 16}, {16, 2, 16}};
     const ResidentVariant *v = nullptr;
     int c = 0;
     switch (n) {
         case 16: case 32: v = v16; c = 1; break;
-        case 64: v = v64; c = 6; break;
-        case 128: v = v128; c = 3; break;
+        case 64: v = v64; c = 8; break;
+        case 128: v = v128; c = 5; break;
         case 256: v = v256; c = 3; break;
         default: return 0;
     }

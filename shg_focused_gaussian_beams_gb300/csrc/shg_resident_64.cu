@@ -17,6 +17,8 @@ SHG_RESIDENT_INSTANTIATE(64, 2, 2, 8)
 SHG_RESIDENT_INSTANTIATE(64, 2, 4, 8)
 SHG_RESIDENT_INSTANTIATE(64, 1, 1, 4)
 SHG_RESIDENT_INSTANTIATE(64, 1, 2, 4)
+SHG_RESIDENT_INSTANTIATE(64, 4, 4, 8)
+SHG_RESIDENT_INSTANTIATE(64, 8, 8, 8)
 
 cudaError_t prepare_resident_small(int n, int cs, int minb, int g, int *m) {
     if (n == 16) return prepare_resident_t<16, 1, 1, 4>(m);
@@ -24,6 +26,8 @@ cudaError_t prepare_resident_small(int n, int cs, int minb, int g, int *m) {
     if (g == 4 && cs == 1 && minb == 1) return prepare_resident_t<64, 1, 1, 4>(m);
     if (g == 4 && cs == 1 && minb == 2) return prepare_resident_t<64, 1, 2, 4>(m);
     if (g != 8) return cudaErrorInvalidValue;
+    if (cs == 4 && minb == 4) return prepare_resident_t<64, 4, 4, 8>(m);
+    if (cs == 8 && minb == 8) return prepare_resident_t<64, 8, 8, 8>(m);
     if (cs == 1 && minb == 1) return prepare_resident_t<64, 1, 1, 8>(m);
     if (cs == 1 && minb == 2) return prepare_resident_t<64, 1, 2, 8>(m);
     if (cs == 2 && minb == 2) return prepare_resident_t<64, 2, 2, 8>(m);
@@ -38,6 +42,8 @@ cudaError_t launch_resident_small(int n, int cs, int minb, int g, const InstDesc
     if (g == 4 && cs == 1 && minb == 1) return launch_resident_t<64, 1, 1, 4>(inst, list, njobs, counter, max_clusters, st);
     if (g == 4 && cs == 1 && minb == 2) return launch_resident_t<64, 1, 2, 4>(inst, list, njobs, counter, max_clusters, st);
     if (g != 8) return cudaErrorInvalidValue;
+    if (cs == 4 && minb == 4) return launch_resident_t<64, 4, 4, 8>(inst, list, njobs, counter, max_clusters, st);
+    if (cs == 8 && minb == 8) return launch_resident_t<64, 8, 8, 8>(inst, list, njobs, counter, max_clusters, st);
     if (cs == 1 && minb == 1) return launch_resident_t<64, 1, 1, 8>(inst, list, njobs, counter, max_clusters, st);
     if (cs == 1 && minb == 2) return launch_resident_t<64, 1, 2, 8>(inst, list, njobs, counter, max_clusters, st);
     if (cs == 2 && minb == 2) return launch_resident_t<64, 2, 2, 8>(inst, list, njobs, counter, max_clusters, st);

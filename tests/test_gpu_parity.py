@@ -138,8 +138,8 @@ def test_errors_are_reported():
         s.cwes(50.0)
 
 
-RESIDENT_VARIANTS = {64: [(1, 1), (1, 2), (2, 2), (2, 4)], 128: [(2, 1), (4, 1), (4, 2)],
-                     256: [(8, 1), (16, 1), (16, 2)]}
+RESIDENT_VARIANTS = {64: [(1, 1), (1, 2), (2, 2), (2, 4), (4, 4), (8, 8)],
+                     128: [(2, 1), (4, 1), (4, 2), (8, 4), (16, 8)], 256: [(8, 1), (16, 1), (16, 2)]}
 
 
 def test_every_schedule_gives_identical_fields():
@@ -156,7 +156,7 @@ def test_every_schedule_gives_identical_fields():
         ref.set_schedule(n, resident=False)
     eta_r, fr = ref.run(with_fields=True)
     ran = {n: 0 for n in RESIDENT_VARIANTS}
-    for k in range(4):
+    for k in range(6):
         sw = Sweep(pick, crystal=W.CRYSTAL_QPM50)
         for n, vs in RESIDENT_VARIANTS.items():
             cs, mb = vs[min(k, len(vs) - 1)]
