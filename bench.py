@@ -370,8 +370,8 @@ def measured_hbm():
 
 
 def ncu_traffic(kernel):
-    """DRAM bytes per grid point of one launch of `kernel` from the committed ncu summary
-    (profiles/ncu_traffic.json), or None."""
+    """Measured DRAM traffic of `kernel` from the committed ncu summaries
+    (profiles/ncu_traffic.json): a dict with bytes per solve or per grid point, or None."""
     p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     try:
         with open(p) as f:
@@ -520,11 +520,19 @@ def run_ours(args):
     peak, peak_kind = measured_hbm()
     achieved = bytes_k / (ms_k * 1e-3) / 1e9
     tr = ncu_traffic(dom)
-    pts_per_launch = bytes_k / n_l / (32.0 if dom.startswith("rows") else 48.0)
+    traffic = None
+    if tr and "bytes_per_solve" in tr and dom.startswith("resident<"):
+        # the resident march moves each solve's fields in and out once (and reads its
+        # propagators from L2): traffic scales with the solves of the launch, not the steps
+        n_dom = int(dom[len("resident<"):-1])
+        traffic = tr["bytes_per_solve"] * sum(1 for i in insts if i.nx == n_dom)
+    elif tr and "bytes_per_point" in tr:
+        traffic = tr["bytes_per_point"] * bytes_k / n_l / (32.0 if dom.startswith("rows") else 48.0)
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": peak_kind, "launches": n_l,
             "ms_per_launch": ms_k / n_l, "algorithmic_bytes_per_launch": bytes_k / n_l,
-            "traffic": None if tr is None else tr * pts_per_launch,
+            "traffic": traffic,
+            "traffic_source": None if tr is None else tr.get("source"),
             "share_of_step": ms_k / sum(v[1] for v in prof.values()),
             "kernels": {k: {"launches": v[0], "ms": v[1], "GBps": v[2] / (v[1] * 1e-3) / 1e9} for k, v in prof.items()}}
 
