@@ -163,7 +163,12 @@ int ensure_twiddles(int device) {
 // A set of plain solves with their device buffers and launch schedule.
 class Batch {
    public:
-    ~Batch() { release(); }
+    ~Batch() {
+        release();
+        for (auto s2 : side_streams_) cudaStreamDestroy(s2);
+        for (auto e2 : side_events_) cudaEventDestroy(e2);
+        if (fork_event_) cudaEventDestroy(fork_event_);
+    }
 
     int create(const shg_config &crystal, const std::vector<SolveParams> &sp) {
         release();
