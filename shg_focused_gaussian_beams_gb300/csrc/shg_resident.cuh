@@ -170,15 +170,16 @@ __global__ void __launch_bounds__(ResShape<N, CS_, MINB_, G_>::THREADS, MINB_)
                         if constexpr (CS > 1) p = cg::this_cluster().map_shared_rank(p, y / R);
                         return p;
                     };
+                    // propagator values first: their L2 latency overlaps the column transform
+                    float2 h[E];
+#pragma unroll
+                    for (int r = 0; r < E; ++r) h[r] = __ldg(H + (size_t)spec_index<N, G>(ct, r) * N + x);
                     float2 v[E];
 #pragma unroll
                     for (int j = 0; j < E; ++j) v[j] = *at(j);
                     fft_nat_to_spec<N, G, +1, true, R, G>(v, ct, scr + cc, tab);
 #pragma unroll
-                    for (int r = 0; r < E; ++r) {
-                        const int k = spec_index<N, G>(ct, r);
-                        v[r] = c_mul(v[r], __ldg(H + (size_t)k * N + x));
-                    }
+                    for (int r = 0; r < E; ++r) v[r] = c_mul(v[r], h[r]);
                     fft_spec_to_nat<N, G, -1, true, R, G>(v, ct, scr + cc, tab);
 #pragma unroll
                     for (int j = 0; j < E; ++j) *at(j) = v[j];
