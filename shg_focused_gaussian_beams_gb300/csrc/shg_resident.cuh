@@ -94,6 +94,8 @@ __global__ void __launch_bounds__(ResShape<N, CS_, MINB_, G_>::THREADS, MINB_)
             // ---- row phase (local rows)
             {
                 float2 *rowP = sP + line * N, *rowS = sS + line * N;
+                // step constants of slices s-1 and s (s <= K < nz), loaded before the transform
+                const float4 cprev = d.stepc[s > 0 ? s - 1 : 0], ccur = d.stepc[s];
                 float2 vp[E], vs[E];
 #pragma unroll
                 for (int j = 0; j < E; ++j) {
@@ -101,7 +103,7 @@ __global__ void __launch_bounds__(ResShape<N, CS_, MINB_, G_>::THREADS, MINB_)
                     vs[j] = rowS[t + G * j];
                 }
                 if (s == 0) {
-                    const float4 c = d.stepc[0];
+                    const float4 c = ccur;
 #pragma unroll
                     for (int j = 0; j < E; ++j) rk4_point(vp[j], vs[j], c, d);
                     fft_nat_to_spec<N, G, +1>(vp, t, rsc, tab);
@@ -116,7 +118,7 @@ __global__ void __launch_bounds__(ResShape<N, CS_, MINB_, G_>::THREADS, MINB_)
                 } else {
                     fft_nat_to_spec<N, G, -1>(vp, t, rsc, tab);
                     fft_nat_to_spec<N, G, -1>(vs, t, rsc, tab);
-                    const float4 c1 = d.stepc[s - 1];
+                    const float4 c1 = cprev;
 #pragma unroll
                     for (int r = 0; r < E; ++r) rk4_point(vp[r], vs[r], c1, d);
                     if (d.slices && s < d.nz) {
@@ -142,7 +144,7 @@ __global__ void __launch_bounds__(ResShape<N, CS_, MINB_, G_>::THREADS, MINB_)
                         block_add_double_res(aS, d.acc + 1);
                         block_add_double_res(aP, d.acc + 2);
                     } else {
-                        const float4 c2 = d.stepc[s];
+                        const float4 c2 = ccur;
 #pragma unroll
                         for (int r = 0; r < E; ++r) rk4_point(vp[r], vs[r], c2, d);
                         fft_spec_to_nat<N, G, +1>(vp, t, rsc, tab);
