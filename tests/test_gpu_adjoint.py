@@ -148,7 +148,8 @@ def _fd_job(args):
 def test_config_adjoint_256x400_full_size():
     """The adjoint workload at full size: 256x256x400, P = 20 W, xi = 2.84, Gaussian pump
     times a seeded 5 % perturbation smooth over 8 cells, 20 checkpoints; FP64 central
-    differences (run in parallel processes) on 4 field directions, T and Lambda."""
+    differences (run in parallel processes) on 32 seeded field directions, T and Lambda, as the
+    adjoint workload specifies."""
     import multiprocessing as mpx
     n, nz = 256, 400
     inst = W.plain_instance(n, nz, 20.0, 2.84, T0)
@@ -165,7 +166,7 @@ def test_config_adjoint_256x400_full_size():
     eps0 = float(np.float32(8.8541878128e-12 * 1e12 / 1e6))
     cl = float(np.float32(299792458 * 1e6 / 1e12))
     kl = 0.5 * eps0 * cl * float(np.float32(inst.lx / (n - 1))) * float(np.float32(inst.ly / (n - 1)))
-    dirs = [smooth_noise(rng, n) * pump for _ in range(4)]
+    dirs = [smooth_noise(rng, n) * pump for _ in range(32)]
     jobs, meta = [], []
     for d in dirs:
         eps = 1e-4 * np.linalg.norm(pump) / np.linalg.norm(d)
