@@ -59,6 +59,72 @@ def loss64(c, pump64, T=T0, lam=None):
     return 0.5 * eps0 * cl * o.n64(0.532, T) * dx * dy * float(np.sum(np.abs(so) ** 2))
 
 
+def torch_loss64(c, pump):
+    """The plain method (Solver.h:65-117, 156-276 with its quirks) in torch complex128, from the
+    same FP64 constants as the oracle's double model (delta-k pinned to the float value):
+    the reference gradient, by torch autograd, of the SH output power."""
+    cfg, o = c["cfg"], c["o"]
+    n, nz = cfg.nx, cfg.nz
+    dev = pump.device
+    pi = 3.14159265358979323846
+    cl, eps0 = 299792458 * 1e6 / 1e12, 8.8541878128e-12 * 1e12 / 1e6
+    lp = float(cfg.lp)
+    ls = 0.5 * lp
+    n_p, n_s = o.n64(lp, T0), o.n64(ls, T0)
+    dq = (2.0 / pi) * float(cfg.deff)
+    kp, ks = pi * dq / (n_p * lp), 0.5 * pi * dq / (n_s * ls)
+    hp, hs = 0.5 * float(cfg.alpha_p), 0.5 * float(cfg.alpha_s)
+    tpa = 0.5 * float(cfg.beta_s) * 0.5 * cl * eps0 * n_s
+    dz = float(cfg.lz) / (nz - 1)
+    hp_shift, hs_shift = (torch.from_numpy(h).to(dev) for h in o.propagators64(T0))
+    dk = c["dk32"]
+
+    def dadz(P, S, ph):
+        e = torch.exp(torch.tensor(-1j * ph, dtype=torch.complex128, device=dev))
+        dP = 1j * kp * S * P.conj() * e - hp * P
+        dS = 1j * ks * P * P * e.conj() - (hs + tpa * (S.abs() ** 2)) * S
+        return dP, dS
+
+    def rk4(P, S, z):
+        ph = z * dk
+        k1 = dadz(P, S, ph)
+        k2 = dadz(P + 0.5 * k1[0], S + 0.5 * k1[1], ph)
+        k3 = dadz(P + 0.5 * k2[0], S + 0.5 * k2[1], ph)
+        k4 = dadz(P + k3[0], S + k3[1], ph)
+        return (P + dz / 6 * (k1[0] + 2 * k2[0] + 2 * k3[0] + k4[0]),
+                S + dz / 6 * (k1[1] + 2 * k2[1] + 2 * k3[1] + k4[1]))
+
+    def diffraction(A, H):
+        return torch.fft.fft2(H * torch.fft.ifft2(A))
+
+    P, S = pump, torch.zeros_like(pump)
+    z = 0.0
+    for _ in range(nz - 1):
+        P, S = rk4(P, S, z)
+        P, S = diffraction(P, hp_shift), diffraction(S, hs_shift)
+        P, S = rk4(P, S, z)
+        z += dz
+    # the loss scale of loss64 (float-rounded eps0 and c, n_s at 0.532 um)
+    eps0f = float(np.float32(8.8541878128e-12 * 1e12 / 1e6))
+    clf = float(np.float32(299792458 * 1e6 / 1e12))
+    dx = float(np.float32(cfg.lx / (n - 1)))
+    dy = float(np.float32(cfg.ly / (n - 1)))
+    return 0.5 * eps0f * clf * o.n64(0.532, T0) * dx * dy * (S.abs() ** 2).sum()
+
+
+def test_gradient_field_vs_torch_fp64_reference(case):
+    """The whole pump-gradient field against torch autograd through a complex128
+    restatement of the method; the restatement's loss is pinned to the oracle's FP64 run."""
+    p = torch.from_numpy(case["pump64"]).cuda().requires_grad_(True)
+    L = torch_loss64(case, p)
+    assert abs(L.item() - loss64(case, case["pump64"])) / L.item() < 1e-9
+    L.backward()
+    ref = p.grad.cpu().numpy()
+    got = case["r"]["grad_pump"].cpu().numpy().astype(np.complex128)
+    rel = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+    assert rel < FD_RTOL, rel
+
+
 def test_loss_matches_fp64(case):
     L = loss64(case, case["pump64"])
     assert abs(case["r"]["loss"] - L) / L < 1e-4
@@ -194,3 +260,8 @@ def test_config_adjoint_256x400_full_size():
             assert abs(r["dLambda"] - fdk) / abs(fdk) < FD_RTOL, (r["dLambda"], fdk)
     adj, fd = np.array(adj), np.array(fd)
     assert np.linalg.norm(adj - fd) / np.linalg.norm(fd) < FD_RTOL, (adj, fd)
+    # the whole gradient field against the complex128 autograd reference
+    p = torch.from_numpy(pump).cuda().requires_grad_(True)
+    torch_loss64({"cfg": cfg, "o": o, "dk32": dk32}, p).backward()
+    ref = p.grad.cpu().numpy()
+    assert np.linalg.norm(g - ref) / np.linalg.norm(ref) < FD_RTOL
