@@ -215,13 +215,17 @@ def run_heat(args):
     vox = inst.nx * inst.ny * inst.nz
     peak, kind = measured_hbm()
     out = {"workload": "heat256: Jacobi sweeps on 256x256x400, oven-surrounded", "peak": peak, "peak_source": kind}
-    for kind in args.heat_kinds.split(","):
+    for spec in args.heat_kinds.split(","):
+        kind, _, zc = spec.partition(":")  # "tma:50" = TMA-staged sweep with 50-plane chunks
         os.environ["SHG_HEAT"] = kind
+        if zc:
+            os.environ["SHG_HEAT_ZC"] = zc
         for lv in args.heat_levels.split(","):
             os.environ["SHG_HEAT_TB"] = lv
             per = heat_sweep_time(inst, max(args.steps, 1) * 96)
-            out[f"{kind}_levels_{lv}"] = {"ms_per_sweep": 1e3 * per, "GBps_algorithmic": 12.0 * vox / per / 1e9,
+            out[f"{spec}_levels_{lv}"] = {"ms_per_sweep": 1e3 * per, "GBps_algorithmic": 12.0 * vox / per / 1e9,
                                           "frac": 12.0 * vox / per / 1e9 / peak}
+        os.environ.pop("SHG_HEAT_ZC", None)
     os.environ.pop("SHG_HEAT_TB")
     os.environ.pop("SHG_HEAT")
     print(json.dumps(out), flush=True)
@@ -261,9 +265,11 @@ def run_thermal(args):
             "config": {"workload": "thermal256: 256x256x400, P=30 W, xi=2.84, 2000x1000 um cross-section, "
                                    "oven-surrounded faces at a seeded U(45,55) C", "t_oven": inst.temp},
             "jacobi_counts": counts, "voxel_sweeps_per_s": vox * sweeps / t,
-            "roofline": {"bound": "hbm", "kernel": "k_heat_ws<1,4> (one Jacobi sweep)", "achieved": ach, "peak": peak, "unit": "GB/s",
+            "roofline": {"bound": "hbm", "kernel": "k_heat_tma<1,4> (one Jacobi sweep: TMA plane ring, 4 rows per "
+                                                   "consumer warp, 8-plane chunks)",
+                         "achieved": ach, "peak": peak, "unit": "GB/s",
                          "frac": ach / peak, "peak_source": peak_kind, "ms_per_launch": 1e3 * per_sweep,
-                         "algorithmic_bytes_per_launch": 12.0 * vox, "traffic": None,
+                         "algorithmic_bytes_per_launch": 12.0 * vox, "traffic": heat_traffic(vox),
                          "note": "CUDA events around 400 back-to-back sweeps on the launching stream"},
             "clocks": clk.summary(), "efficiency": s.efficiency()}
     # the workload's relative-residual stop rule (||dT|| / ||T|| < 1e-6, checked every 100 sweeps)
@@ -378,6 +384,13 @@ def ncu_traffic(kernel):
             return json.load(f).get(kernel)
     except (OSError, ValueError):
         return None
+
+
+def heat_traffic(vox):
+    """DRAM bytes of one TMA-staged sweep over `vox` voxels from the committed ncu capture
+    (bytes per voxel of a 256x256x400 launch), or None."""
+    t = ncu_traffic("heat_tma<4>")
+    return None if t is None else t["bytes_per_voxel"] * vox
 
 
 def dist_setup(n_gpus):
@@ -570,7 +583,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--heat-levels", default="1", help="heat256: sweeps per launch to time (1 = no blocking)")
-    ap.add_argument("--heat-kinds", default="ws8", help="heat256: single-sweep kernels to time (ws8, ws4, 25)")
+    ap.add_argument("--heat-kinds", default="tma,ws4",
+                    help="heat256: single-sweep kernels to time (tma, tma:<planes per block>, ws4, ws8, 25)")
     ap.add_argument("--workload", choices=["sweep", "plain128", "rows256", "thermal256", "heat256", "adjoint256", "thermal_adjoint",
                                               "resident256"],
                     default="sweep")

@@ -53,6 +53,11 @@ cudaError_t launch_heat_tb(float *Tf, const float *Ti, const float *QK, const He
 int heat_levels();
 cudaError_t verify_fast_division(float d, float r, unsigned long long *d_count, unsigned long long *mismatches,
                                  cudaStream_t st);
+// shg_heat_tma.cu: the TMA-staged sweep (NX % 4 == 0) and its pipeline error flag.
+bool heat_tma_supported(int nx, int ny, int nz);
+cudaError_t launch_heat_tma(float *Tf, const float *Ti, const float *QK, const HeatCoef &c, int nx, int ny, int nz,
+                            int bc, cudaStream_t st, int rows_per_warp = 1);
+cudaError_t heat_tma_error(int *flag, cudaStream_t st);
 cudaError_t launch_sq_diff_sum(const float *Tf, const float *Ti, size_t n, double *out, cudaStream_t st);
 cudaError_t launch_sq_sums(const float *Tf, const float *Ti, size_t n, double *out2, cudaStream_t st);
 cudaError_t launch_sellmeier_tables(const float *T, float *NP, float *NS, float *DK, size_t n, float lp, float ls,

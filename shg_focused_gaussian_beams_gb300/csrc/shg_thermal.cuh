@@ -98,4 +98,97 @@ __device__ __forceinline__ void rk4_point_th(float2 &P, float2 &S, const ThCoef 
     S = make_float2(fmaf(accs.x, d.dz6, S.x), fmaf(accs.y, d.dz6, S.y));
 }
 
+// ---- one voxel of the heat stencil (shared by the sweep kernels) ----------------------
+
+// a / d for the interior stencil: the corrected product where it was verified equal to the
+// IEEE quotient, IEEE division otherwise.
+__device__ __forceinline__ float div_const(float a, float d, float r, int fast) {
+    const unsigned e = (__float_as_uint(a) >> 23) & 0xffu;
+    if (fast && e - kDivExpLo <= kDivExpHi - kDivExpLo) {
+        const float q = a * r;
+        const float rem = fmaf(-q, d, a);
+        return fmaf(rem, r, q);
+    }
+    return __fdiv_rn(a, d);
+}
+
+// One voxel of Tfield.h:113-258 from its six face neighbours (only those the formula of
+// the voxel's class uses are read): xm/xp, ym/yp, zm/zp = T at x-1/x+1, y-1/y+1, z-1/z+1.
+// Returns false for voxels the reference never writes.
+template <int BC>
+__device__ __forceinline__ bool heat_voxel(const HeatCoef &c, int x, int y, int z, int nx, int ny, int nz, float xm,
+                                           float xp, float ym, float yp, float zm, float zp, float qk, float &out) {
+    const bool xi = x > 0 && x < nx - 1, yi = y > 0 && y < ny - 1, zi = z > 0 && z < nz - 1;
+    if (xi && yi && zi) {
+        const float a = div_const(__fadd_rn(xp, xm), c.dx2, c.rdx2, c.fast_div);
+        const float b = div_const(__fadd_rn(yp, ym), c.dy2, c.rdy2, c.fast_div);
+        const float d = div_const(__fadd_rn(zp, zm), c.dz2, c.rdz2, c.fast_div);
+        out = __fmul_rn(c.L2, __fadd_rn(__fadd_rn(__fadd_rn(a, b), d), qk));
+        return true;
+    }
+    const float tzn = z == 0 ? zp : zm;
+    if (xi && yi) {  // back / front faces
+        float s = __fadd_rn(tzn, __fmul_rn(c.az, __fadd_rn(xp, xm)));
+        s = __fadd_rn(s, __fmul_rn(c.bz, __fadd_rn(yp, ym)));
+        s = __fadd_rn(s, c.tinfBiz);
+        out = __fdiv_rn(s, c.den_z);
+        return true;
+    }
+    if (BC != 0) return false;
+    const bool xe = x == 0 || x == nx - 1, ze = z == 0 || z == nz - 1, ytop = y == ny - 1;
+    const float txn = x == 0 ? xp : xm;
+    if (xe && yi && zi) {
+        float s = __fadd_rn(txn, __fmul_rn(c.ax, __fadd_rn(yp, ym)));
+        s = __fadd_rn(s, __fmul_rn(c.bx, __fadd_rn(zp, zm)));
+        s = __fadd_rn(s, c.tinfBix);
+        out = __fdiv_rn(s, c.den_x);
+    } else if (xi && ytop && zi) {
+        float s = __fadd_rn(ym, __fmul_rn(c.ay, __fadd_rn(xp, xm)));
+        s = __fadd_rn(s, __fmul_rn(c.by, __fadd_rn(zp, zm)));
+        s = __fadd_rn(s, c.tinfBiy);
+        out = __fdiv_rn(s, c.den_y);
+    } else if (xe && yi && ze) {
+        const float s = __fadd_rn(__fadd_rn(__fmul_rn(c.av, txn), __fmul_rn(c.bv, tzn)), __fmul_rn(c.cv, __fadd_rn(yp, ym)));
+        out = __double2float_rn(__dmul_rn(__dadd_rn((double)s, c.KV), (double)c.V));
+    } else if (ytop && xi && ze) {
+        const float s = __fadd_rn(__fadd_rn(__fmul_rn(c.ah, ym), __fmul_rn(c.bh, tzn)), __fmul_rn(c.ch, __fadd_rn(xm, xp)));
+        out = __double2float_rn(__dmul_rn(__dadd_rn((double)s, c.KH), (double)c.H));
+    } else if (xe && ytop && zi) {
+        const float s = __fadd_rn(__fadd_rn(__fmul_rn(c.ad, ym), __fmul_rn(c.bd, txn)), __fmul_rn(c.cd, __fadd_rn(zp, zm)));
+        out = __double2float_rn(__dmul_rn(__dadd_rn((double)s, c.KD), (double)c.D));
+    } else if (xe && ytop && ze) {
+        float s = __fadd_rn(__fmul_rn(c.AV, txn), __fmul_rn(c.BV, ym));
+        s = __fadd_rn(s, __fmul_rn(c.CV, tzn));
+        s = __fadd_rn(s, c.tinfBiD);
+        out = __fmul_rn(s, c.GV);
+    } else {
+        return false;
+    }
+    return true;
+}
+
+// Interior voxel (Tfield.h:132) with the three divisions by dx^2, dy^2, dz^2 taken as
+// corrected products when all three numerators lie in the verified exponent range (one
+// combined test), else through div_const: bit-identical to heat_voxel's interior branch.
+__device__ __forceinline__ bool div_in_range(float a) {
+    return ((__float_as_uint(a) & 0x7f800000u) - (kDivExpLo << 23)) <= ((kDivExpHi - kDivExpLo) << 23);
+}
+
+__device__ __forceinline__ float interior_voxel(const HeatCoef &c, float xm, float xp, float ym, float yp, float zm,
+                                                float zp, float qk) {
+    const float sx = __fadd_rn(xp, xm), sy = __fadd_rn(yp, ym), sz = __fadd_rn(zp, zm);
+    float a, b, d;
+    if (c.fast_div && div_in_range(sx) && div_in_range(sy) && div_in_range(sz)) {
+        const float qa = sx * c.rdx2, qb = sy * c.rdy2, qd = sz * c.rdz2;
+        a = fmaf(fmaf(-qa, c.dx2, sx), c.rdx2, qa);
+        b = fmaf(fmaf(-qb, c.dy2, sy), c.rdy2, qb);
+        d = fmaf(fmaf(-qd, c.dz2, sz), c.rdz2, qd);
+    } else {
+        a = div_const(sx, c.dx2, c.rdx2, c.fast_div);
+        b = div_const(sy, c.dy2, c.rdy2, c.fast_div);
+        d = div_const(sz, c.dz2, c.rdz2, c.fast_div);
+    }
+    return __fmul_rn(c.L2, __fadd_rn(__fadd_rn(__fadd_rn(a, b), d), qk));
+}
+
 }  // namespace shg

@@ -176,7 +176,24 @@ int ThermalSolve::sweeps(float t_inf, int n) {
 
 // Solver.h:302-324: the residual is checked after the first sweep and then after every
 // 5000th; the loop stops when it is below 5e-4/TSIZE or equal to the previous check.
+// A TMA-staged sweep whose pipeline gave up leaves its error flag set: report it.
+static int heat_pipeline_ok(cudaStream_t st) {
+    int flag = 0;
+    TH_CUDA(heat_tma_error(&flag, st));
+    if (flag) {
+        set_error("heat sweep: a TMA pipeline wait gave up (sweep incomplete)");
+        return SHG_ERR_CUDA;
+    }
+    return SHG_OK;
+}
+
 int ThermalSolve::jacobi(float t_inf, int *counter) {
+    const int rc = jacobi_run(t_inf, counter);
+    if (rc) return rc;
+    return heat_pipeline_ok(st_);
+}
+
+int ThermalSolve::jacobi_run(float t_inf, int *counter) {
     if (rel_tol_ > 0) {
         // relative residual of one sweep, every check_every sweeps
         int c = 0;
@@ -425,7 +442,7 @@ int shg_heat_sweeps_device(const shg_config *cfg, void *Ta, void *Tb, const void
         TH_CUDA(launch_heat(b, a, static_cast<const float *>(QK), hc, cfg->nx, cfg->ny, cfg->nz, bc, st));
         std::swap(a, b);
     }
-    return SHG_OK;
+    return heat_pipeline_ok(st);
 }
 
 int shg_dk_thermal(const shg_config *cfg, const float *T, float *DK, float *NP, float *NS) {

@@ -68,6 +68,7 @@ class ThermalSolve {
 
    private:
     int sq_diff(float *out);
+    int jacobi_run(float t_inf, int *counter);
     shg_config cfg_{};
     int n_ = 0, nz_ = 0, bc_ = 0;
     size_t tsize_ = 0;

@@ -56,16 +56,22 @@ def test_heat_sweeps_bitexact_vs_oracle_random():
     assert bits_equal(D, o.dk_thermal(T))
 
 
-@pytest.mark.parametrize("kind,levels", [("ws8", "1"), ("ws4", "1"), ("ws4b", "1"), ("25", "1"), ("simple", "1"), ("ws4", "2"),
-                                         ("ws4", "3"), ("ws4", "4")])
-def test_heat_kernels_bitexact(kind, levels, monkeypatch):
-    """Every heat-sweep kernel (warp strips of 8 or 4 rows, the 2.5D tile, the plain
-    kernel) and K sweeps per launch (temporal blocking) equal the reference's sweeps bit for
-    bit: a grid that no tile size divides, sweep counts around multiples of K, both BC modes."""
+@pytest.mark.parametrize("kind,levels,shape", [("ws8", "1", (40, 40, 33)), ("ws4", "1", (40, 40, 33)),
+                                               ("ws4b", "1", (40, 40, 33)), ("tma", "1", (40, 40, 33)),
+                                               ("tma", "1", (44, 44, 35)), ("tma1", "1", (44, 44, 35)),
+                                               ("tma2", "1", (44, 44, 35)), ("tma8", "1", (44, 44, 35)),
+                                               ("tma8", "1", (72, 72, 9)), ("25", "1", (40, 40, 33)),
+                                               ("simple", "1", (40, 40, 33)), ("ws4", "2", (40, 40, 33)),
+                                               ("ws4", "3", (40, 40, 33)), ("ws4", "4", (40, 40, 33))])
+def test_heat_kernels_bitexact(kind, levels, shape, monkeypatch):
+    """Every heat-sweep kernel (warp strips of 8 or 4 rows, the TMA-staged tile, the 2.5D
+    tile, the plain kernel) and K sweeps per launch (temporal blocking) equal the reference's
+    sweeps bit for bit: grids that the tile sizes do not divide (nx x ny x nz given),
+    sweep counts around multiples of K, both BC modes."""
     monkeypatch.setenv("SHG_HEAT", kind)
     monkeypatch.setenv("SHG_HEAT_TB", levels)
-    n, nz = 40, 33
-    cfg = O.make_cfg(W.CRYSTAL_QPM50, n, n, nz, 600.0, 600.0)
+    nx, ny, nz = shape
+    cfg = O.make_cfg(W.CRYSTAL_QPM50, nx, ny, nz, 600.0, 600.0)
     o = O.Oracle(cfg)
     rng = np.random.default_rng(11)
     for bc in (0, 1):
