@@ -60,7 +60,8 @@ def test_heat_sweeps_bitexact_vs_oracle_random():
                                                ("ws4b", "1", (40, 40, 33)), ("tma", "1", (40, 40, 33)),
                                                ("tma", "1", (44, 44, 35)), ("tma1", "1", (44, 44, 35)),
                                                ("tma2", "1", (44, 44, 35)), ("tma8", "1", (44, 44, 35)),
-                                               ("tma8", "1", (72, 72, 9)), ("25", "1", (40, 40, 33)),
+                                               ("tma8", "1", (72, 72, 9)), ("tma4", "1", (136, 136, 11)),
+                                               ("25", "1", (40, 40, 33)),
                                                ("simple", "1", (40, 40, 33)), ("ws4", "2", (40, 40, 33)),
                                                ("ws4", "3", (40, 40, 33)), ("ws4", "4", (40, 40, 33))])
 def test_heat_kernels_bitexact(kind, levels, shape, monkeypatch):
