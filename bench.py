@@ -541,8 +541,22 @@ def run_ours(args):
         traffic = tr["bytes_per_solve"] * sum(1 for i in insts if i.nx == n_dom)
     elif tr and "bytes_per_point" in tr:
         traffic = tr["bytes_per_point"] * bytes_k / n_l / (32.0 if dom.startswith("rows") else 48.0)
+    issue = None
+    if tr and "thread_inst_per_pt_step" in tr:
+        # the resident march keeps its fields on chip, so its bound is FP32 instruction issue:
+        # thread-instructions per second (ncu count per pt.step x the launch's pt.steps from
+        # its algorithmic bytes, 32 B per pt.step) against the issue peak of 4 schedulers x
+        # 32 lanes per SM at the sampled SM clock
+        props = torch.cuda.get_device_properties(local)
+        pt_steps = bytes_k / n_l / 32.0
+        inst_s = tr["thread_inst_per_pt_step"] * pt_steps / (ms_k / n_l * 1e-3)
+        sm_mhz = clk.summary().get("sm_mhz") or 2070.0
+        peak_inst = props.multi_processor_count * 128 * sm_mhz * 1e6
+        issue = {"achieved": inst_s, "peak": peak_inst, "unit": "thread-instructions/s", "frac": inst_s / peak_inst,
+                 "thread_inst_per_pt_step": tr["thread_inst_per_pt_step"], "source": tr.get("inst_source"),
+                 "peak_note": f"{props.multi_processor_count} SMs x 128 lanes x {sm_mhz:.0f} MHz (nominal issue rate)"}
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_source": peak_kind, "launches": n_l,
+            "frac": achieved / peak, "peak_source": peak_kind, "launches": n_l, "issue": issue,
             "ms_per_launch": ms_k / n_l, "algorithmic_bytes_per_launch": bytes_k / n_l,
             "traffic": traffic,
             "traffic_source": None if tr is None else tr.get("source"),
