@@ -485,107 +485,128 @@ __device__ __forceinline__ void block_add_double_th(double v, double *dst) {
     }
 }
 
+// Block shape: LPB lines, one thread per point (LPB * N threads). The row transforms run on
+// 2 * LPB * G threads (the pump's lines on the first LPB * G, the SH's on the next), the
+// per-point RK4 and heat source on all threads with the point in natural x order, so the
+// per-voxel loads are coalesced and the coupling arithmetic is spread over N threads per
+// line instead of G.
 template <int N>
 struct ThRowShape {
     static constexpr int G = LineShape<N>::G;
-    static constexpr int TPB = (N * G < 256) ? N * G : 256;
-    static constexpr int LPB = TPB / G;
+    static constexpr int LPB = (512 / N < N) ? 512 / N : N;  // lines per block (N = 16: all 16)
+    static constexpr int TPB = LPB * N;
     static constexpr int BPI = N / LPB;
+    static_assert(LPB >= 1 && N % LPB == 0, "whole lines per block");
+    static constexpr int FFT_THREADS = LPB * G;  // per field
+    static_assert(FFT_THREADS % 32 == 0 && 2 * FFT_THREADS <= TPB, "transform threads fill whole warps");
 };
 
 template <int N>
 __global__ void __launch_bounds__(ThRowShape<N>::TPB) k_rows_th(const InstDesc *__restrict__ dd, const ThermDesc th, int s) {
-    constexpr int G = LineShape<N>::G, E = N / G, LPB = ThRowShape<N>::LPB;
+    using Sh = ThRowShape<N>;
+    constexpr int G = Sh::G, E = N / G, LPB = Sh::LPB, FT = Sh::FFT_THREADS;
     constexpr int SC = LineScratch<N, G>::SIZE;
-    __shared__ float2 scratch[LPB * SC];
+    __shared__ float2 scratch[2 * LPB * SC];
+    __shared__ float2 lines[2][LPB * N];  // [field][line * N + x], natural x order
     const InstDesc &d = *dd;
     const float2 *__restrict__ tab = g_twiddle + N;
-    const int y = blockIdx.x * LPB + threadIdx.x / G;
-    const int t = threadIdx.x % G;
-    float2 *sc = scratch + (threadIdx.x / G) * SC;
-    const size_t base = (size_t)y * N;
     const size_t nxy = (size_t)N * N;
-    float2 vp[E], vs[E];
-#pragma unroll
-    for (int j = 0; j < E; ++j) {
-        vp[j] = d.P[base + t + G * j];
-        vs[j] = d.S[base + t + G * j];
-    }
+    const int tid = threadIdx.x;
+    // transform role: field f, line fl, thread t of the line
+    const bool xf = tid < 2 * FT;
+    const int f = tid / FT, fl = (tid % FT) / G, t = tid % G;
+    float2 *const F = f == 0 ? d.P : d.S;
+    float2 *const fline = lines[f & 1] + fl * N;
+    float2 *const fsc = scratch + (size_t)((f & 1) * LPB + fl) * SC;
+    const size_t fbase = (size_t)(blockIdx.x * LPB + fl) * N;
+    // point role: line l, column x
+    const int l = tid / N, x = tid % N;
+    const size_t i2 = (size_t)(blockIdx.x * LPB + l) * N + x;
+    float2 *const pP = lines[0] + l * N + x, *const pS = lines[1] + l * N + x;
+
     if (s == 0) {
+        // DKint = DK(slice 0); RK4 of step 0; then the backward transform along x
+        float2 vp = d.P[i2], vs = d.S[i2];
+        const float dkint = th.DK[i2];
+        th.DKint[i2] = dkint;
+        const ThCoef k = th_coef(th, th.NP[i2], th.NS[i2], dkint, 0, d.dz);
+        rk4_point_th(vp, vs, k, d);
+        *pP = vp;
+        *pS = vs;
+        __syncthreads();
+        if (xf) {
+            float2 v[E];
 #pragma unroll
-        for (int j = 0; j < E; ++j) {
-            const size_t i2 = base + t + G * j;
-            const float dkint = th.DK[i2];
-            th.DKint[i2] = dkint;
-            const ThCoef k = th_coef(th, th.NP[i2], th.NS[i2], dkint, 0, d.dz);
-            rk4_point_th(vp[j], vs[j], k, d);
-        }
-        fft_nat_to_spec<N, G, +1>(vp, t, sc, tab);
-        fft_nat_to_spec<N, G, +1>(vs, t, sc, tab);
+            for (int j = 0; j < E; ++j) v[j] = fline[t + G * j];
+            fft_nat_to_spec<N, G, +1>(v, t, fsc, tab);
 #pragma unroll
-        for (int r = 0; r < E; ++r) {
-            const int kx = spec_index<N, G>(t, r);
-            d.P[base + kx] = vp[r];
-            d.S[base + kx] = vs[r];
+            for (int r = 0; r < E; ++r) F[fbase + spec_index<N, G>(t, r)] = v[r];
         }
         return;
     }
-    fft_nat_to_spec<N, G, -1>(vp, t, sc, tab);
-    fft_nat_to_spec<N, G, -1>(vs, t, sc, tab);
+    // forward transform of the rows into natural x order
+    if (xf) {
+        float2 v[E];
+#pragma unroll
+        for (int j = 0; j < E; ++j) v[j] = F[fbase + t + G * j];
+        fft_nat_to_spec<N, G, -1>(v, t, fsc, tab);
+#pragma unroll
+        for (int r = 0; r < E; ++r) fline[spec_index<N, G>(t, r)] = v[r];
+    }
+    __syncthreads();
     const bool capture = (s == th.nz - 1);
     double aS = 0.0, aP = 0.0;
-#pragma unroll
-    for (int r = 0; r < E; ++r) {
-        const int x = spec_index<N, G>(t, r);
-        const size_t i2 = base + x, i3 = (size_t)(s - 1) * nxy + i2;
+    {
+        float2 vp = *pP, vs = *pS;
+        const size_t i3 = (size_t)(s - 1) * nxy + i2;
         const float np1 = th.NP[i3], ns1 = th.NS[i3];
         const float dkint = th.DKint[i2];
         const ThCoef k1 = th_coef(th, np1, ns1, dkint, s - 1, d.dz);
-        rk4_point_th(vp[r], vs[r], k1, d);
+        rk4_point_th(vp, vs, k1, d);
         // Tfield.h:277-290: heat source of slice s-1 from the fields after step s-1
-        const float a2p = fmaf(vp[r].x, vp[r].x, vp[r].y * vp[r].y);
-        const float a2s = fmaf(vs[r].x, vs[r].x, vs[r].y * vs[r].y);
+        const float a2p = fmaf(vp.x, vp.x, vp.y * vp.y);
+        const float a2s = fmaf(vs.x, vs.x, vs.y * vs.y);
         const float Ip = th.qc * np1 * a2p, Is = th.qc * ns1 * a2s;
         const float Q = th.alpha_p * Ip + th.alpha_s * Is + th.beta_s * (Is * Is);
         th.QK[i3] = Q / th.kth;
         if (d.slices && s < th.nz) {
             float2 *sl = d.slices + (size_t)s * 2 * nxy;
-            sl[i2] = vp[r];
-            sl[nxy + i2] = vs[r];
+            sl[i2] = vp;
+            sl[nxy + i2] = vs;
         }
         if (capture) {
-            d.Pout[i2] = vp[r];
-            d.Sout[i2] = vs[r];
-            aS += (double)a2s;
-            aP += (double)a2p;
+            d.Pout[i2] = vp;
+            d.Sout[i2] = vs;
+            aS = (double)a2s;
+            aP = (double)a2p;
         }
         if (s < th.nz) {
             const size_t i3n = (size_t)s * nxy + i2;
             const float dk2 = dkint + th.DK[i3n];
             th.DKint[i2] = dk2;
             const ThCoef k2 = th_coef(th, th.NP[i3n], th.NS[i3n], dk2, s, d.dz);
-            rk4_point_th(vp[r], vs[r], k2, d);
+            rk4_point_th(vp, vs, k2, d);
+            *pP = vp;
+            *pS = vs;
+        } else {
+            d.P[i2] = vp;
+            d.S[i2] = vs;
         }
     }
     if (capture) {
         block_add_double_th(aS, d.acc + 1);
         block_add_double_th(aP, d.acc + 2);
     }
-    if (s == th.nz) {
+    if (s == th.nz) return;
+    __syncthreads();
+    // backward transform along x back to the column pass's layout
+    if (xf) {
+        float2 v[E];
 #pragma unroll
-        for (int r = 0; r < E; ++r) {
-            const int kx = spec_index<N, G>(t, r);
-            d.P[base + kx] = vp[r];
-            d.S[base + kx] = vs[r];
-        }
-        return;
-    }
-    fft_spec_to_nat<N, G, +1>(vp, t, sc, tab);
-    fft_spec_to_nat<N, G, +1>(vs, t, sc, tab);
+        for (int r = 0; r < E; ++r) v[r] = fline[spec_index<N, G>(t, r)];
+        fft_spec_to_nat<N, G, +1>(v, t, fsc, tab);
 #pragma unroll
-    for (int j = 0; j < E; ++j) {
-        d.P[base + t + G * j] = vp[j];
-        d.S[base + t + G * j] = vs[j];
+        for (int j = 0; j < E; ++j) F[fbase + t + G * j] = v[j];
     }
 }
 
