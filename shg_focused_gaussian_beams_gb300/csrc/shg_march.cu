@@ -194,33 +194,31 @@ __global__ void __launch_bounds__(RowShape<N>::TPB) k_rows(const InstDesc *__res
 }
 
 // Column pass. Block = TC columns x G threads (lane = column + TC * t) so that every
-// load and store is a run of TC consecutive complex values.
-template <int N>
-__global__ void __launch_bounds__(16 * LineShape<N>::G) k_cols(const InstDesc *__restrict__ inst, const int *__restrict__ list) {
-    constexpr int G = LineShape<N>::G, E = N / G, TC = 16, BPI = N / TC;
+// load and store is a run of TC consecutive complex values; blockIdx.y = field (pump, SH).
+template <int N, int TC>
+__global__ void __launch_bounds__(TC * LineShape<N>::G) k_cols(const InstDesc *__restrict__ inst, const int *__restrict__ list) {
+    constexpr int G = LineShape<N>::G, E = N / G, BPI = N / TC;
     __shared__ float2 scratch[TC * E * G];
     const InstDesc &d = inst[list[blockIdx.x / BPI]];
     const float2 *__restrict__ tab = g_twiddle + N;
     const int c = threadIdx.x % TC, t = threadIdx.x / TC;
     const int x = (blockIdx.x % BPI) * TC + c;
     float2 *sc = scratch + c;
-#pragma unroll 1
-    for (int f = 0; f < 2; ++f) {
-        float2 *F = f == 0 ? d.P : d.S;
-        const float2 *__restrict__ H = f == 0 ? d.Hp : d.Hs;
-        float2 v[E];
+    const int f = blockIdx.y;
+    float2 *F = f == 0 ? d.P : d.S;
+    const float2 *__restrict__ H = f == 0 ? d.Hp : d.Hs;
+    float2 v[E];
 #pragma unroll
-        for (int j = 0; j < E; ++j) v[j] = F[(size_t)(t + G * j) * N + x];
-        fft_nat_to_spec<N, G, +1, true, TC, G>(v, t, sc, tab);
+    for (int j = 0; j < E; ++j) v[j] = F[(size_t)(t + G * j) * N + x];
+    fft_nat_to_spec<N, G, +1, true, TC, G>(v, t, sc, tab);
 #pragma unroll
-        for (int r = 0; r < E; ++r) {
-            const int k = spec_index<N, G>(t, r);
-            v[r] = c_mul(v[r], __ldg(H + (size_t)k * N + x));
-        }
-        fft_spec_to_nat<N, G, -1, true, TC, G>(v, t, sc, tab);
-#pragma unroll
-        for (int j = 0; j < E; ++j) F[(size_t)(t + G * j) * N + x] = v[j];
+    for (int r = 0; r < E; ++r) {
+        const int k = spec_index<N, G>(t, r);
+        v[r] = c_mul(v[r], __ldg(H + (size_t)k * N + x));
     }
+    fft_spec_to_nat<N, G, -1, true, TC, G>(v, t, sc, tab);
+#pragma unroll
+    for (int j = 0; j < E; ++j) F[(size_t)(t + G * j) * N + x] = v[j];
 }
 
 // ---------------------------------------------------------------------------------------
@@ -314,11 +312,16 @@ static cudaError_t launch_rows_t(const InstDesc *inst, const int *list, int coun
     return cudaGetLastError();
 }
 
+// 16-column tiles when several solves fill the GPU; 4-column tiles (four times the blocks)
+// for one to three solves, where the launch would otherwise cover a few SMs.
 template <int N>
 static cudaError_t launch_cols_t(const InstDesc *inst, const int *list, int count, cudaStream_t st) {
-    constexpr int G = LineShape<N>::G, TC = 16, BPI = N / TC;
+    constexpr int G = LineShape<N>::G;
     if (count <= 0) return cudaSuccess;
-    k_cols<N><<<count * BPI, TC * G, 0, st>>>(inst, list);
+    if (count >= 4)
+        k_cols<N, 16><<<dim3(count * (N / 16), 2), 16 * G, 0, st>>>(inst, list);
+    else
+        k_cols<N, 4><<<dim3(count * (N / 4), 2), 4 * G, 0, st>>>(inst, list);
     return cudaGetLastError();
 }
 
