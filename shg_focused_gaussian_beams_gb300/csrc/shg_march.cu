@@ -193,6 +193,95 @@ __global__ void __launch_bounds__(RowShape<N>::TPB) k_rows(const InstDesc *__res
     }
 }
 
+// Row pass for one to three solves: the same work as k_rows with one thread per point.
+// Block = LPB lines x N threads; the row transforms run on 2 * LPB * G threads (pump lines
+// first, then SH lines), both RK4 calls on every thread for its point through a
+// shared-memory line buffer, so a lone solve occupies N * N threads instead of N * G.
+template <int N>
+struct PtRowShape {
+    static constexpr int G = LineShape<N>::G;
+    static constexpr int LPB = (512 / N < N) ? 512 / N : N;
+    static constexpr int TPB = LPB * N;
+    static constexpr int BPI = N / LPB;
+    static constexpr int FT = LPB * G;  // transform threads per field
+    static_assert(FT % 32 == 0 && 2 * FT <= TPB && N % LPB == 0, "transform threads fill whole warps");
+};
+
+template <int N>
+__global__ void __launch_bounds__(PtRowShape<N>::TPB) k_rows_pt(const InstDesc *__restrict__ inst, const int *__restrict__ list, int s) {
+    using Sh = PtRowShape<N>;
+    constexpr int G = Sh::G, E = N / G, LPB = Sh::LPB, BPI = Sh::BPI, FT = Sh::FT;
+    constexpr int SC = LineScratch<N, G>::SIZE;
+    __shared__ float2 scratch[2 * LPB * SC];
+    __shared__ float2 lines[2][LPB * N];  // [field][line * N + x], natural x order
+    const InstDesc &d = inst[list[blockIdx.x / BPI]];
+    const float2 *__restrict__ tab = g_twiddle + N;
+    const int tid = threadIdx.x, line0 = (blockIdx.x % BPI) * LPB;
+    // transform role
+    const bool xf = tid < 2 * FT;
+    const int f = tid / FT, fl = (tid % FT) / G, t = tid % G;
+    float2 *const F = f == 0 ? d.P : d.S;
+    float2 *const fline = lines[f & 1] + fl * N;
+    float2 *const fsc = scratch + (size_t)((f & 1) * LPB + fl) * SC;
+    const size_t fbase = (size_t)(line0 + fl) * N;
+    // point role
+    const int l = tid / N, x = tid % N;
+    const size_t i2 = (size_t)(line0 + l) * N + x;
+    float2 *const pP = lines[0] + l * N + x, *const pS = lines[1] + l * N + x;
+
+    if (s == 0) {
+        float2 vp = d.P[i2], vs = d.S[i2];
+        rk4_point(vp, vs, d.stepc[0], d);
+        *pP = vp;
+        *pS = vs;
+        __syncthreads();
+        if (xf) {
+            float2 v[E];
+#pragma unroll
+            for (int j = 0; j < E; ++j) v[j] = fline[t + G * j];
+            fft_nat_to_spec<N, G, +1>(v, t, fsc, tab);
+#pragma unroll
+            for (int r = 0; r < E; ++r) F[fbase + spec_index<N, G>(t, r)] = v[r];
+        }
+        return;
+    }
+    if (xf) {
+        float2 v[E];
+#pragma unroll
+        for (int j = 0; j < E; ++j) v[j] = F[fbase + t + G * j];
+        fft_nat_to_spec<N, G, -1>(v, t, fsc, tab);
+#pragma unroll
+        for (int r = 0; r < E; ++r) fline[spec_index<N, G>(t, r)] = v[r];
+    }
+    __syncthreads();
+    float2 vp = *pP, vs = *pS;
+    rk4_point(vp, vs, d.stepc[s - 1], d);
+    if (d.slices && s < d.nz) {
+        float2 *sl = d.slices + (size_t)s * 2 * N * N;
+        sl[i2] = vp;
+        sl[(size_t)N * N + i2] = vs;
+    }
+    if (s == d.nsteps) {
+        d.Pout[i2] = vp;
+        d.Sout[i2] = vs;
+        block_add_double((double)vs.x * vs.x + (double)vs.y * vs.y, d.acc + 1);
+        block_add_double((double)vp.x * vp.x + (double)vp.y * vp.y, d.acc + 2);
+        return;
+    }
+    rk4_point(vp, vs, d.stepc[s], d);
+    *pP = vp;
+    *pS = vs;
+    __syncthreads();
+    if (xf) {
+        float2 v[E];
+#pragma unroll
+        for (int r = 0; r < E; ++r) v[r] = fline[spec_index<N, G>(t, r)];
+        fft_spec_to_nat<N, G, +1>(v, t, fsc, tab);
+#pragma unroll
+        for (int j = 0; j < E; ++j) F[fbase + t + G * j] = v[j];
+    }
+}
+
 // Column pass. Block = TC columns x G threads (lane = column + TC * t) so that every
 // load and store is a run of TC consecutive complex values; blockIdx.y = field (pump, SH).
 template <int N, int TC>
@@ -308,7 +397,10 @@ int rows_threads() { return 256; }
 template <int N>
 static cudaError_t launch_rows_t(const InstDesc *inst, const int *list, int count, int s, cudaStream_t st) {
     if (count <= 0) return cudaSuccess;
-    k_rows<N><<<count * RowShape<N>::BPI, RowShape<N>::TPB, 0, st>>>(inst, list, s);
+    if (count >= 4)
+        k_rows<N><<<count * RowShape<N>::BPI, RowShape<N>::TPB, 0, st>>>(inst, list, s);
+    else
+        k_rows_pt<N><<<count * PtRowShape<N>::BPI, PtRowShape<N>::TPB, 0, st>>>(inst, list, s);
     return cudaGetLastError();
 }
 
