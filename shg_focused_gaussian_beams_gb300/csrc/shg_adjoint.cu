@@ -25,73 +25,6 @@ const float2 *twiddle_symbol_address_adjoint() {
     return static_cast<const float2 *>(p);
 }
 
-// Forward RK4 on a plain state (Solver.h:216-228 with the step constants folded).
-__global__ void k_rk4_state(float2 *P, float2 *S, int nn, const float4 *__restrict__ stepc, int s,
-                            const InstDesc *__restrict__ dd) {
-    const InstDesc &d = *dd;
-    const float4 c = stepc[s];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += gridDim.x * blockDim.x) {
-        float2 p = P[i], q = S[i];
-        rk4_point(p, q, c, d);
-        P[i] = p;
-        S[i] = q;
-    }
-}
-
-// RK4^T at the base state (P0, S0): (cP, cS) hold the cotangent of the RK4 output on
-// entry and of its input on exit. acc_step[0..4] += the step's sensitivities.
-__global__ void k_rk4_vjp(const float2 *__restrict__ P0, const float2 *__restrict__ S0, float2 *cP, float2 *cS,
-                          int nn, const float4 *__restrict__ stepc, int s, const InstDesc *__restrict__ dd,
-                          double *acc_step) {
-    const InstDesc &d = *dd;
-    const float4 c = stepc[s];
-    const float hp = d.hp, t0 = d.tpa0, t1 = d.tpa1, w6 = d.dz6;
-    double acc[5] = {0, 0, 0, 0, 0};
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += gridDim.x * blockDim.x) {
-        const float2 P = P0[i], S = S0[i];
-        // forward stages
-        float2 k1p, k1s, k2p, k2s, k3p, k3s;
-        dadz_point(P, S, c, hp, t0, t1, k1p, k1s);
-        const float2 B2p = make_float2(fmaf(0.5f, k1p.x, P.x), fmaf(0.5f, k1p.y, P.y));
-        const float2 B2s = make_float2(fmaf(0.5f, k1s.x, S.x), fmaf(0.5f, k1s.y, S.y));
-        dadz_point(B2p, B2s, c, hp, t0, t1, k2p, k2s);
-        const float2 B3p = make_float2(fmaf(0.5f, k2p.x, P.x), fmaf(0.5f, k2p.y, P.y));
-        const float2 B3s = make_float2(fmaf(0.5f, k2s.x, S.x), fmaf(0.5f, k2s.y, S.y));
-        dadz_point(B3p, B3s, c, hp, t0, t1, k3p, k3s);
-        const float2 B4p = c_add(P, k3p), B4s = c_add(S, k3s);
-        // reverse
-        const float2 op = cP[i], os = cS[i];
-        float2 cap = op, cas = os;
-        float2 ck3p = make_float2(2.0f * w6 * op.x, 2.0f * w6 * op.y), ck3s = make_float2(2.0f * w6 * os.x, 2.0f * w6 * os.y);
-        float2 ck2p = ck3p, ck2s = ck3s;
-        float2 ck1p = make_float2(w6 * op.x, w6 * op.y), ck1s = make_float2(w6 * os.x, w6 * os.y);
-        const float2 ck4p = ck1p, ck4s = ck1s;
-        float2 bp = make_float2(0.f, 0.f), bs = make_float2(0.f, 0.f);
-        dadz_vjp(B4p, B4s, ck4p, ck4s, c, hp, t0, t1, bp, bs, acc);
-        cap = c_add(cap, bp);
-        cas = c_add(cas, bs);
-        ck3p = c_add(ck3p, bp);
-        ck3s = c_add(ck3s, bs);
-        bp = bs = make_float2(0.f, 0.f);
-        dadz_vjp(B3p, B3s, ck3p, ck3s, c, hp, t0, t1, bp, bs, acc);
-        cap = c_add(cap, bp);
-        cas = c_add(cas, bs);
-        ck2p = make_float2(fmaf(0.5f, bp.x, ck2p.x), fmaf(0.5f, bp.y, ck2p.y));
-        ck2s = make_float2(fmaf(0.5f, bs.x, ck2s.x), fmaf(0.5f, bs.y, ck2s.y));
-        bp = bs = make_float2(0.f, 0.f);
-        dadz_vjp(B2p, B2s, ck2p, ck2s, c, hp, t0, t1, bp, bs, acc);
-        cap = c_add(cap, bp);
-        cas = c_add(cas, bs);
-        ck1p = make_float2(fmaf(0.5f, bp.x, ck1p.x), fmaf(0.5f, bp.y, ck1p.y));
-        ck1s = make_float2(fmaf(0.5f, bs.x, ck1s.x), fmaf(0.5f, bs.y, ck1s.y));
-        bp = bs = make_float2(0.f, 0.f);
-        dadz_vjp(P, S, ck1p, ck1s, c, hp, t0, t1, bp, bs, acc);
-        cP[i] = c_add(cap, bp);
-        cS[i] = c_add(cas, bs);
-    }
-    block_sum_doubles(acc, 5, acc_step);
-}
-
 // Column pass of the diffraction step on one field of one solve (after the row transform
 // along x with sign +1): backward transform along y, then either
 //   MODE 0 (forward):  store the 2D spectrum F (if Fst), multiply by H', forward along y;
@@ -102,10 +35,12 @@ __global__ void k_rk4_vjp(const float2 *__restrict__ P0, const float2 *__restric
 //   MODE 2 (adjoint, no sums): multiply by conj(H'), forward.
 // All fields of all solves in one launch: blockIdx.y = 2*solve + {0 pump (Hp), 1 SH (Hs)};
 // A and Fst hold the fields back to back (solve-major), acc[blockIdx.y] receives the sums.
-template <int N, int MODE>
-__global__ void __launch_bounds__(16 * LineShape<N>::G) k_colpass(float2 *A0, float2 *Fst0,
+// TC columns per block: 16 when several solves fill the GPU, 4 for one to three solves
+// (N >= 64, so that a block holds whole warps).
+template <int N, int MODE, int TC>
+__global__ void __launch_bounds__(TC * LineShape<N>::G) k_colpass(float2 *A0, float2 *Fst0,
                                                              const InstDesc *__restrict__ dd, double *acc0) {
-    constexpr int G = LineShape<N>::G, E = N / G, TC = 16;
+    constexpr int G = LineShape<N>::G, E = N / G;
     __shared__ float2 scratch[TC * E * G];
     const float2 *__restrict__ tab = g_twiddle + N;
     const int f = blockIdx.y;
@@ -116,16 +51,24 @@ __global__ void __launch_bounds__(16 * LineShape<N>::G) k_colpass(float2 *A0, fl
     const float2 *__restrict__ H = (f & 1) ? d.Hs : d.Hp;
     double *acc = acc0 ? acc0 + f : nullptr;
     const int c = threadIdx.x % TC, t = threadIdx.x / TC, x = blockIdx.x * TC + c;
+    // propagator values (and the stored spectrum) first: their latency overlaps the transform
+    float2 hv[E], fv[MODE == 1 ? E : 1];
+#pragma unroll
+    for (int r = 0; r < E; ++r) {
+        const size_t i = (size_t)spec_index<N, G>(t, r) * N + x;
+        hv[r] = __ldg(H + i);
+        if constexpr (MODE == 1) fv[r] = Fst[i];
+    }
     float2 v[E];
 #pragma unroll
     for (int j = 0; j < E; ++j) v[j] = A[(size_t)(t + G * j) * N + x];
     fft_nat_to_spec<N, G, +1, true, TC, G>(v, t, scratch + c, tab);
-    double a = 0.0;
+    float a = 0.0f;  // this thread's E terms; FP64 across threads
 #pragma unroll
     for (int r = 0; r < E; ++r) {
         const int k = spec_index<N, G>(t, r);
         const size_t i = (size_t)k * N + x;
-        const float2 h = __ldg(H + i);
+        const float2 h = hv[r];
         if (MODE == 0) {
             if (Fst) Fst[i] = v[r];
             v[r] = c_mul(v[r], h);
@@ -135,19 +78,187 @@ __global__ void __launch_bounds__(16 * LineShape<N>::G) k_colpass(float2 *A0, fl
             const int ux = (x + N / 2) & (N - 1), uy = (k + N / 2) & (N - 1);
             const float tx = (float)ux - d.uX, ty = (float)uy - d.uY;
             const float q2 = d.dfX2 * (tx * tx) + d.dfY2 * (ty * ty);
-            const float2 fx = c_mulc(Fst[i], v[r]);   // F conj(X)
+            const float2 fx = c_mulc(fv[MODE == 1 ? r : 0], v[r]);   // F conj(X)
             const float2 fh = c_mul(fx, h);
-            a += -(double)fh.y * (double)q2;          // Re(i z) = -Im(z)
+            a = fmaf(-fh.y, q2, a);                   // Re(i z) = -Im(z)
             v[r] = c_mulc(v[r], h);                   // conj(H') X
         }
     }
     fft_spec_to_nat<N, G, -1, true, TC, G>(v, t, scratch + c, tab);
 #pragma unroll
     for (int j = 0; j < E; ++j) A[(size_t)(t + G * j) * N + x] = v[j];
-    if (MODE == 1) {
-        double b[1] = {a};
-        block_sum_doubles(b, 1, acc);
+    if (MODE == 1) block_sum_f2d(&a, 1, acc);
+}
+
+// ---------------------------------------------------------------------------------------
+// Fused row passes for one solve, one thread per point (block = LPB lines x N threads; the
+// x-transforms of the pump and SH lines run on two groups of LPB * G threads). Between two
+// column passes a row pass finishes one diffraction along x, applies the pointwise RK4 (or
+// RK4^T) work of the step boundary, and starts the next diffraction along x, so a z-step
+// costs one row and one column launch. The working state A / cotangent C holds the pump
+// then the SH field (n*n each); the column passes (k_colpass) see rows in natural
+// frequency order, as after launch_dft_rows(+1).
+template <int N>
+struct AdjRowShape {
+    static constexpr int G = LineShape<N>::G;
+    static constexpr int LPB = (512 / N < N) ? 512 / N : N;
+    static constexpr int TPB = LPB * N;
+    static constexpr int BPI = N / LPB;
+    static constexpr int FT = LPB * G;  // transform threads per field
+    static_assert(FT % 32 == 0 && 2 * FT <= TPB && N % LPB == 0, "transform threads fill whole warps");
+};
+
+// Shared state of a fused row pass: line buffers and the roles of this thread.
+template <int N>
+struct AdjRowCtx {
+    using Sh = AdjRowShape<N>;
+    static constexpr int G = Sh::G, E = N / G, LPB = Sh::LPB, FT = Sh::FT, SC = LineScratch<N, G>::SIZE;
+    float2 *fline, *fsc;  // transform role: this thread's line buffer and FFT scratch
+    int t;
+    bool xf;
+    size_t frow;          // offset of the transformed row in A (field included)
+    size_t i2;            // point role: index of the point in one field
+    int lx;               // point role: offset in a line buffer
+    __device__ AdjRowCtx(float2 (*lines)[LPB * N], float2 *scratch) {
+        const int tid = threadIdx.x, line0 = blockIdx.x * LPB;
+        xf = tid < 2 * FT;
+        const int f = (tid / FT) & 1, fl = (tid % FT) / G;
+        t = tid % G;
+        fline = lines[f] + fl * N;
+        fsc = scratch + (size_t)(f * LPB + fl) * SC;
+        frow = (size_t)f * N * N + (size_t)(line0 + fl) * N;
+        const int l = tid / N, x = tid % N;
+        i2 = (size_t)(line0 + l) * N + x;
+        lx = l * N + x;
     }
+    // rows of A (natural frequency order) -> line buffers in real space (natural x order)
+    __device__ void finish(const float2 *A, const float2 *tab) {
+        if (xf) {
+            float2 v[E];
+#pragma unroll
+            for (int j = 0; j < E; ++j) v[j] = A[frow + t + G * j];
+            fft_nat_to_spec<N, G, -1>(v, t, fsc, tab);
+#pragma unroll
+            for (int r = 0; r < E; ++r) fline[spec_index<N, G>(t, r)] = v[r];
+        }
+    }
+    // line buffers (real space) -> rows of A in natural frequency order
+    __device__ void start(float2 *A, const float2 *tab) {
+        if (xf) {
+            float2 v[E];
+#pragma unroll
+            for (int r = 0; r < E; ++r) v[r] = fline[spec_index<N, G>(t, r)];
+            fft_spec_to_nat<N, G, +1>(v, t, fsc, tab);
+#pragma unroll
+            for (int j = 0; j < E; ++j) A[frow + t + G * j] = v[j];
+        }
+    }
+};
+
+// Forward row pass at step boundary s (0 <= s <= K):
+//   finish (s > 0): W_{s-1} = end of the diffraction of step s-1 -> w_out; X_s = RK4(W_{s-1})
+//   else          : X_s = (inP, inS)
+//   X_s -> x_out, ck_out (when given); start (s < K): Y_s = RK4(X_s), begin the diffraction
+//   of step s; else X_K -> final_out.
+// Stored states hold the pump then the SH field, natural layout.
+template <int N>
+__global__ void __launch_bounds__(AdjRowShape<N>::TPB)
+    k_adj_rows_fwd(const InstDesc *__restrict__ dd, float2 *A, int s, int finish, int start, const float2 *inP,
+                   const float2 *inS, float2 *w_out, float2 *x_out, float2 *ck_out, float2 *final_out) {
+    using Cx = AdjRowCtx<N>;
+    __shared__ float2 scratch[2 * Cx::LPB * Cx::SC];
+    __shared__ float2 lines[2][Cx::LPB * N];
+    const InstDesc &d = *dd;
+    const float2 *__restrict__ tab = g_twiddle + N;
+    const size_t nn = (size_t)N * N;
+    Cx cx(lines, scratch);
+    float2 p, q;
+    if (finish) {
+        cx.finish(A, tab);
+        __syncthreads();
+        p = lines[0][cx.lx];
+        q = lines[1][cx.lx];
+        if (w_out) {
+            w_out[cx.i2] = p;
+            w_out[nn + cx.i2] = q;
+        }
+        rk4_point(p, q, d.stepc[s - 1], d);
+    } else {
+        p = inP[cx.i2];
+        q = inS[cx.i2];
+    }
+    if (x_out) {
+        x_out[cx.i2] = p;
+        x_out[nn + cx.i2] = q;
+    }
+    if (ck_out) {
+        ck_out[cx.i2] = p;
+        ck_out[nn + cx.i2] = q;
+    }
+    if (!start) {
+        final_out[cx.i2] = p;
+        final_out[nn + cx.i2] = q;
+        return;
+    }
+    rk4_point(p, q, d.stepc[s], d);
+    lines[0][cx.lx] = p;  // each point thread rewrites only the entry it read
+    lines[1][cx.lx] = q;
+    __syncthreads();
+    cx.start(A, tab);
+}
+
+// Backward row pass at step boundary s (-1 <= s < K), cotangent C:
+//   finish: end of the adjoint diffraction of step s+1, then c_{X_{s+1}} = RK4^T(X_{s+1})[c]
+//           (sums into acc_fin, the step s+1 row of acc_step)
+//   else  : c = C (natural layout)
+//   start : c_{W_s} = RK4^T(W_s)[c] (sums into acc_start), begin the adjoint diffraction of
+//           step s; else c -> C (natural layout).
+template <int N>
+__global__ void __launch_bounds__(AdjRowShape<N>::TPB)
+    k_adj_rows_bwd(const InstDesc *__restrict__ dd, float2 *C, int s, int finish, int start,
+                   const float2 *__restrict__ Xn, const float2 *__restrict__ Wn, double *acc_fin, double *acc_start) {
+    using Cx = AdjRowCtx<N>;
+    __shared__ float2 scratch[2 * Cx::LPB * Cx::SC];
+    __shared__ float2 lines[2][Cx::LPB * N];
+    const InstDesc &d = *dd;
+    const float2 *__restrict__ tab = g_twiddle + N;
+    const size_t nn = (size_t)N * N;
+    const float hp = d.hp, t0 = d.tpa0, t1 = d.tpa1, w6 = d.dz6;
+    Cx cx(lines, scratch);
+    float a1[5] = {0, 0, 0, 0, 0}, a2[5] = {0, 0, 0, 0, 0};  // this point's sums, FP64 across points
+    // the stored states of this point first: their latency overlaps the transform
+    float2 xp = make_float2(0.f, 0.f), xs = xp, wp = xp, ws = xp;
+    if (finish) {
+        xp = Xn[cx.i2];
+        xs = Xn[nn + cx.i2];
+    }
+    if (start) {
+        wp = Wn[cx.i2];
+        ws = Wn[nn + cx.i2];
+    }
+    float2 cp, cs;
+    if (finish) {
+        cx.finish(C, tab);
+        __syncthreads();
+        cp = lines[0][cx.lx];
+        cs = lines[1][cx.lx];
+        rk4_vjp_point(xp, xs, cp, cs, d.stepc[s + 1], hp, t0, t1, w6, a1);
+    } else {
+        cp = C[cx.i2];
+        cs = C[nn + cx.i2];
+    }
+    if (start) {
+        rk4_vjp_point(wp, ws, cp, cs, d.stepc[s], hp, t0, t1, w6, a2);
+        lines[0][cx.lx] = cp;  // each point thread rewrites only the entry it read
+        lines[1][cx.lx] = cs;
+        __syncthreads();
+        cx.start(C, tab);
+    } else {
+        C[cx.i2] = cp;
+        C[nn + cx.i2] = cs;
+    }
+    if (finish) block_sum_f2d(a1, 5, acc_fin);
+    if (start) block_sum_f2d(a2, 5, acc_start);
 }
 
 // sum |S|^2 of a field (FP64).
@@ -175,30 +286,26 @@ static int grid_for(int nn) {
     return b < 1216 ? b : 1216;
 }
 
-cudaError_t launch_rk4_state(float2 *P, float2 *S, int nn, const float4 *stepc, int s, const InstDesc *d,
-                             cudaStream_t st) {
-    k_rk4_state<<<grid_for(nn), 256, 0, st>>>(P, S, nn, stepc, s, d);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_rk4_vjp(const float2 *P0, const float2 *S0, float2 *cP, float2 *cS, int nn, const float4 *stepc,
-                           int s, const InstDesc *d, double *acc_step, cudaStream_t st) {
-    k_rk4_vjp<<<grid_for(nn), 256, 0, st>>>(P0, S0, cP, cS, nn, stepc, s, d, acc_step);
+template <int N, int TC>
+static cudaError_t launch_colpass_tc(int mode, float2 *A, float2 *F, const InstDesc *d, double *acc, int solves,
+                                     cudaStream_t st) {
+    constexpr int G = LineShape<N>::G;
+    const dim3 grid(N / TC, 2 * solves);
+    if (mode == 0)
+        k_colpass<N, 0, TC><<<grid, TC * G, 0, st>>>(A, F, d, acc);
+    else if (mode == 1)
+        k_colpass<N, 1, TC><<<grid, TC * G, 0, st>>>(A, F, d, acc);
+    else
+        k_colpass<N, 2, TC><<<grid, TC * G, 0, st>>>(A, F, d, acc);
     return cudaGetLastError();
 }
 
 template <int N>
 static cudaError_t launch_colpass_t(int mode, float2 *A, float2 *F, const InstDesc *d, double *acc, int solves,
                                     cudaStream_t st) {
-    constexpr int G = LineShape<N>::G, TC = 16;
-    const dim3 grid(N / TC, 2 * solves);
-    if (mode == 0)
-        k_colpass<N, 0><<<grid, TC * G, 0, st>>>(A, F, d, acc);
-    else if (mode == 1)
-        k_colpass<N, 1><<<grid, TC * G, 0, st>>>(A, F, d, acc);
-    else
-        k_colpass<N, 2><<<grid, TC * G, 0, st>>>(A, F, d, acc);
-    return cudaGetLastError();
+    // narrow tiles only where a block still fills a warp (the sums use full-warp shuffles)
+    if (solves >= 4 || 4 * LineShape<N>::G < 32) return launch_colpass_tc<N, 16>(mode, A, F, d, acc, solves, st);
+    return launch_colpass_tc<N, 4>(mode, A, F, d, acc, solves, st);
 }
 
 cudaError_t launch_colpass(int n, int mode, float2 *A, float2 *F, const InstDesc *d, double *acc, cudaStream_t st,
@@ -210,6 +317,51 @@ cudaError_t launch_colpass(int n, int mode, float2 *A, float2 *F, const InstDesc
         case 64: return launch_colpass_t<64>(mode, A, F, d, acc, solves, st);
         case 128: return launch_colpass_t<128>(mode, A, F, d, acc, solves, st);
         case 256: return launch_colpass_t<256>(mode, A, F, d, acc, solves, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+template <int N>
+static cudaError_t launch_adj_rows_fwd_t(const InstDesc *d, float2 *A, int s, int finish, int start, const float2 *inP,
+                                         const float2 *inS, float2 *w_out, float2 *x_out, float2 *ck_out,
+                                         float2 *final_out, cudaStream_t st) {
+    k_adj_rows_fwd<N><<<AdjRowShape<N>::BPI, AdjRowShape<N>::TPB, 0, st>>>(d, A, s, finish, start, inP, inS, w_out,
+                                                                            x_out, ck_out, final_out);
+    return cudaGetLastError();
+}
+
+template <int N>
+static cudaError_t launch_adj_rows_bwd_t(const InstDesc *d, float2 *C, int s, int finish, int start,
+                                         const float2 *Xn, const float2 *Wn, double *acc_fin, double *acc_start,
+                                         cudaStream_t st) {
+    k_adj_rows_bwd<N><<<AdjRowShape<N>::BPI, AdjRowShape<N>::TPB, 0, st>>>(d, C, s, finish, start, Xn, Wn, acc_fin,
+                                                                            acc_start);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adj_rows_fwd(int n, const InstDesc *d, float2 *A, int s, int finish, int start, const float2 *inP,
+                                const float2 *inS, float2 *w_out, float2 *x_out, float2 *ck_out, float2 *final_out,
+                                cudaStream_t st) {
+    if ((!finish && (!inP || !inS)) || (!start && !final_out)) return cudaErrorInvalidValue;
+    switch (n) {
+        case 16: return launch_adj_rows_fwd_t<16>(d, A, s, finish, start, inP, inS, w_out, x_out, ck_out, final_out, st);
+        case 32: return launch_adj_rows_fwd_t<32>(d, A, s, finish, start, inP, inS, w_out, x_out, ck_out, final_out, st);
+        case 64: return launch_adj_rows_fwd_t<64>(d, A, s, finish, start, inP, inS, w_out, x_out, ck_out, final_out, st);
+        case 128: return launch_adj_rows_fwd_t<128>(d, A, s, finish, start, inP, inS, w_out, x_out, ck_out, final_out, st);
+        case 256: return launch_adj_rows_fwd_t<256>(d, A, s, finish, start, inP, inS, w_out, x_out, ck_out, final_out, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_adj_rows_bwd(int n, const InstDesc *d, float2 *C, int s, int finish, int start, const float2 *Xn,
+                                const float2 *Wn, double *acc_fin, double *acc_start, cudaStream_t st) {
+    if ((finish && (!Xn || !acc_fin)) || (start && (!Wn || !acc_start))) return cudaErrorInvalidValue;
+    switch (n) {
+        case 16: return launch_adj_rows_bwd_t<16>(d, C, s, finish, start, Xn, Wn, acc_fin, acc_start, st);
+        case 32: return launch_adj_rows_bwd_t<32>(d, C, s, finish, start, Xn, Wn, acc_fin, acc_start, st);
+        case 64: return launch_adj_rows_bwd_t<64>(d, C, s, finish, start, Xn, Wn, acc_fin, acc_start, st);
+        case 128: return launch_adj_rows_bwd_t<128>(d, C, s, finish, start, Xn, Wn, acc_fin, acc_start, st);
+        case 256: return launch_adj_rows_bwd_t<256>(d, C, s, finish, start, Xn, Wn, acc_fin, acc_start, st);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -26,10 +26,29 @@ __device__ __forceinline__ void block_sum_doubles(double *v, int k, double *dst)
     }
 }
 
+// Adds the block's k per-thread FP32 partial sums (k <= 5, blockDim <= 512) to dst[0..k)
+// in FP64: the partials are staged in shared memory and warp j sums quantity j in double,
+// so a thread converts 512/32 values of one quantity instead of reducing five doubles.
+__device__ __forceinline__ void block_sum_f2d(const float *v, int k, double *dst) {
+    __shared__ float stage[5][512];
+    const int tid = threadIdx.x, w = tid >> 5, l = tid & 31, nt = blockDim.x;
+    __syncthreads();  // earlier users of the stage are done
+    for (int j = 0; j < k; ++j) stage[j][tid] = v[j];
+    __syncthreads();
+    if (w < k) {
+        double a = 0.0;
+        for (int i = l; i < nt; i += 32) a += (double)stage[w][i];
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (l == 0 && a != 0.0) atomicAdd(dst + w, a);
+    }
+}
+
 // Reverse mode of one dA/dz evaluation at (P, S) with output cotangents (u, v); adds the
-// input cotangents to (cp, cs) and the parameter sensitivities to acc.
+// input cotangents to (cp, cs) and the parameter sensitivities to acc (T = double, or
+// float for the per-point partial sums that a block then reduces in FP64).
+template <typename T>
 __device__ __forceinline__ void dadz_vjp(float2 P, float2 S, float2 u, float2 v, float4 c, float hp, float tpa0,
-                                         float tpa1, float2 &cp, float2 &cs, double *acc) {
+                                         float tpa1, float2 &cp, float2 &cs, T *acc) {
     const float2 aP = make_float2(c.x, c.y), aS = make_float2(c.z, c.w);
     // c_P = -hp u + aP S conj(u) + 2 conj(aS) conj(P) v
     const float2 aPS = c_mul(aP, S);
@@ -50,11 +69,58 @@ __device__ __forceinline__ void dadz_vjp(float2 P, float2 S, float2 u, float2 v,
     const float2 hS = c_mul(P, P);
     const float2 eP = c_mulc(u, gP);                       // u conj(g)
     const float2 eS = c_mulc(v, hS);                       // v conj(h)
-    acc[0] += (double)eP.x;
-    acc[1] += (double)eP.y;
-    acc[2] += (double)eS.x;
-    acc[3] += (double)eS.y;
-    acc[4] += -(double)a2 * ((double)v.x * S.x + (double)v.y * S.y);
+    acc[0] += (T)eP.x;
+    acc[1] += (T)eP.y;
+    acc[2] += (T)eS.x;
+    acc[3] += (T)eS.y;
+    acc[4] += -(T)a2 * ((T)v.x * (T)S.x + (T)v.y * (T)S.y);
+}
+
+// RK4^T of Solver.h:216-228 at the base state (P, S) with step constants c: (cP, cS) hold
+// the cotangent of the RK4 output on entry and of its input on exit; acc[0..4] += the
+// step's sensitivities.
+template <typename T>
+__device__ __forceinline__ void rk4_vjp_point(float2 P, float2 S, float2 &cP, float2 &cS, float4 c, float hp,
+                                              float t0, float t1, float w6, T *acc) {
+    // forward stages
+    float2 k1p, k1s, k2p, k2s, k3p, k3s;
+    dadz_point(P, S, c, hp, t0, t1, k1p, k1s);
+    const float2 B2p = make_float2(fmaf(0.5f, k1p.x, P.x), fmaf(0.5f, k1p.y, P.y));
+    const float2 B2s = make_float2(fmaf(0.5f, k1s.x, S.x), fmaf(0.5f, k1s.y, S.y));
+    dadz_point(B2p, B2s, c, hp, t0, t1, k2p, k2s);
+    const float2 B3p = make_float2(fmaf(0.5f, k2p.x, P.x), fmaf(0.5f, k2p.y, P.y));
+    const float2 B3s = make_float2(fmaf(0.5f, k2s.x, S.x), fmaf(0.5f, k2s.y, S.y));
+    dadz_point(B3p, B3s, c, hp, t0, t1, k3p, k3s);
+    const float2 B4p = c_add(P, k3p), B4s = c_add(S, k3s);
+    // reverse
+    const float2 op = cP, os = cS;
+    float2 cap = op, cas = os;
+    float2 ck3p = make_float2(2.0f * w6 * op.x, 2.0f * w6 * op.y), ck3s = make_float2(2.0f * w6 * os.x, 2.0f * w6 * os.y);
+    float2 ck2p = ck3p, ck2s = ck3s;
+    float2 ck1p = make_float2(w6 * op.x, w6 * op.y), ck1s = make_float2(w6 * os.x, w6 * os.y);
+    const float2 ck4p = ck1p, ck4s = ck1s;
+    float2 bp = make_float2(0.f, 0.f), bs = make_float2(0.f, 0.f);
+    dadz_vjp(B4p, B4s, ck4p, ck4s, c, hp, t0, t1, bp, bs, acc);
+    cap = c_add(cap, bp);
+    cas = c_add(cas, bs);
+    ck3p = c_add(ck3p, bp);
+    ck3s = c_add(ck3s, bs);
+    bp = bs = make_float2(0.f, 0.f);
+    dadz_vjp(B3p, B3s, ck3p, ck3s, c, hp, t0, t1, bp, bs, acc);
+    cap = c_add(cap, bp);
+    cas = c_add(cas, bs);
+    ck2p = make_float2(fmaf(0.5f, bp.x, ck2p.x), fmaf(0.5f, bp.y, ck2p.y));
+    ck2s = make_float2(fmaf(0.5f, bs.x, ck2s.x), fmaf(0.5f, bs.y, ck2s.y));
+    bp = bs = make_float2(0.f, 0.f);
+    dadz_vjp(B2p, B2s, ck2p, ck2s, c, hp, t0, t1, bp, bs, acc);
+    cap = c_add(cap, bp);
+    cas = c_add(cas, bs);
+    ck1p = make_float2(fmaf(0.5f, bp.x, ck1p.x), fmaf(0.5f, bp.y, ck1p.y));
+    ck1s = make_float2(fmaf(0.5f, bs.x, ck1s.x), fmaf(0.5f, bs.y, ck1s.y));
+    bp = bs = make_float2(0.f, 0.f);
+    dadz_vjp(P, S, ck1p, ck1s, c, hp, t0, t1, bp, bs, acc);
+    cP = c_add(cap, bp);
+    cS = c_add(cas, bs);
 }
 
 }  // namespace shg

@@ -8,15 +8,22 @@
 
 namespace shg {
 
-cudaError_t launch_rk4_state(float2 *P, float2 *S, int nn, const float4 *stepc, int s, const InstDesc *d,
-                             cudaStream_t st);
-cudaError_t launch_rk4_vjp(const float2 *P0, const float2 *S0, float2 *cP, float2 *cS, int nn, const float4 *stepc,
-                           int s, const InstDesc *d, double *acc_step, cudaStream_t st);
 // Column pass of the diffraction over `solves` solves (d[solves], fields solve-major):
 // mode 0 forward (spectra into F when F != nullptr), 1 adjoint with the propagator
 // sums into acc[2*solves], 2 adjoint without sums.
 cudaError_t launch_colpass(int n, int mode, float2 *A, float2 *F, const InstDesc *d, double *acc, cudaStream_t st,
                            int solves = 1);
+// Fused row passes of one solve (one row launch per step boundary, see shg_adjoint.cu):
+// forward at boundary s (finish the diffraction of step s-1 and RK4 into X_s, or take X_s
+// from inP / inS; store W_{s-1}, X_s where asked; RK4 and start step s, or store X_K);
+// backward at boundary s (finish the adjoint diffraction of step s+1 and RK4^T at X_{s+1},
+// or take the cotangent from C; RK4^T at W_s and start the adjoint diffraction of step s, or
+// store the cotangent). States and cotangents hold the pump then the SH field.
+cudaError_t launch_adj_rows_fwd(int n, const InstDesc *d, float2 *A, int s, int finish, int start, const float2 *inP,
+                                const float2 *inS, float2 *w_out, float2 *x_out, float2 *ck_out, float2 *final_out,
+                                cudaStream_t st);
+cudaError_t launch_adj_rows_bwd(int n, const InstDesc *d, float2 *C, int s, int finish, int start, const float2 *Xn,
+                                const float2 *Wn, double *acc_fin, double *acc_start, cudaStream_t st);
 cudaError_t launch_abs2_sum(const float2 *S, int nn, double *out, cudaStream_t st);
 cudaError_t launch_seed_cotangent(const float2 *S, float2 *cP, float2 *cS, int nn, const double *g, cudaStream_t st);
 
@@ -28,6 +35,8 @@ struct AdjointWork {
     int n = 0, K = 0, L = 0, nck = 0;
     cudaGraphExec_t graph = nullptr;  // the captured gradient pass for (n, K, L) and graph_key
     cudaStream_t cap = nullptr;       // capture stream
+    cudaStream_t side = nullptr;      // second branch of the captured pass (segment replays)
+    cudaEvent_t ev = nullptr;         // fork / join of the two branches
     const void *graph_key[4] = {};    // device descriptor, P, S, step constants it was captured on
     void *mem = nullptr;
     size_t bytes = 0;

@@ -35,6 +35,8 @@ namespace shg {
 AdjointWork::~AdjointWork() {
     release();
     if (cap) cudaStreamDestroy(cap);
+    if (side) cudaStreamDestroy(side);
+    if (ev) cudaEventDestroy(ev);
 }
 
 void AdjointWork::release() {
@@ -47,8 +49,9 @@ void AdjointWork::release() {
 }
 
 // Layout: X, cot (one state each: P then S), nck checkpoint states, and L segment states
-// for each of X_s, W_s, F_s; then per-step sums (K x 8 doubles) and 8 global doubles
-// ([0..1] propagator sums, [2] sum |S_out|^2, [3] seed scale).
+// for each of X_s, W_s, F_s (two sets of L when checkpointing, so that the replay of one
+// segment overlaps the backward sweep of the next); then per-step sums (K x 8 doubles) and
+// 8 global doubles ([0..1] propagator sums, [2] sum |S_out|^2, [3] seed scale).
 int AdjointWork::ensure(int n_, int K_, int L_, int nck_) {
     if (mem && n == n_ && K == K_ && L == L_ && nck == nck_) return SHG_OK;
     release();
@@ -58,7 +61,8 @@ int AdjointWork::ensure(int n_, int K_, int L_, int nck_) {
     nck = nck_;
     const size_t nn = (size_t)n * n;
     const size_t st = 2 * nn;
-    bytes = sizeof(float2) * (st * (2 + (size_t)nck + 3 * (size_t)L)) + sizeof(double) * (8 * (size_t)K + 8);
+    const size_t sets = nck > 0 ? 2 : 1;
+    bytes = sizeof(float2) * (st * (2 + (size_t)nck + 3 * sets * (size_t)L)) + sizeof(double) * (8 * (size_t)K + 8);
     AD_CUDA(cudaMalloc(&mem, bytes));
     float2 *p = reinterpret_cast<float2 *>(mem);
     X = p;
@@ -68,11 +72,11 @@ int AdjointWork::ensure(int n_, int K_, int L_, int nck_) {
     ck = p;
     p += st * nck;
     Xs = p;
-    p += st * L;
+    p += st * L * sets;
     Ws = p;
-    p += st * L;
+    p += st * L * sets;
     Fs = p;
-    p += st * L;
+    p += st * L * sets;
     acc_step = reinterpret_cast<double *>(p);
     acc_glob = acc_step + 8 * (size_t)K;
     return SHG_OK;
@@ -92,80 +96,78 @@ static double sellmeier_dT(double L, double T) {
     return dn2 / (2 * std::sqrt(n2));
 }
 
-// X <- D(X) for both fields (stored back to back); spectra into F when F != nullptr.
-static int diffraction_fwd(int n, float2 *X, float2 *F, const InstDesc *d, cudaStream_t st) {
-    AD_CUDA(launch_dft_rows(n, +1, X, X, st, 2));
-    AD_CUDA(launch_colpass(n, 0, X, F, d, nullptr, st));
-    AD_CUDA(launch_dft_rows(n, -1, X, X, st, 2));
-    return SHG_OK;
-}
-
-// c <- D^H(c) for both fields, propagator sensitivities added to acc[0], acc[1].
-static int diffraction_adj(int n, float2 *c, float2 *F, const InstDesc *d, double *acc, cudaStream_t st) {
-    AD_CUDA(launch_dft_rows(n, +1, c, c, st, 2));
-    AD_CUDA(launch_colpass(n, 1, c, F, d, acc, st));
-    AD_CUDA(launch_dft_rows(n, -1, c, c, st, 2));
-    return SHG_OK;
-}
-
-static int rk4_state(int n, float2 *X, const InstDesc &h, const InstDesc *d, int s, cudaStream_t st) {
-    const int nn = n * n;
-    AD_CUDA(launch_rk4_state(X, X + nn, nn, h.stepc, s, d, st));
-    return SHG_OK;
-}
-
 // The whole gradient pass on `st`, from the input fields in h.P / h.S to the cotangent of
 // the inputs in w.cot and the sums in w.acc_step / w.acc_glob (seed scale read from
-// w.acc_glob[3]). Segments of L steps; with L == 1 and as many checkpoints as steps the
-// forward pass keeps every step's X_s, W_s, F_s and the backward pass needs no replay.
+// w.acc_glob[3]). Each z-step is one fused row launch and one column launch per direction
+// (launch_adj_rows_fwd / launch_adj_rows_bwd around launch_colpass). Segments of L steps;
+// with store_all the forward pass keeps every step's X_s, W_s, F_s and the backward pass
+// needs no replay.
 static int enqueue_pass(const InstDesc &h, const InstDesc *d, AdjointWork &w, int L, int nseg, bool store_all,
                         cudaStream_t st) {
     const int n = h.n, K = h.nsteps;
-    const size_t nn = (size_t)n * n, sb = 2 * nn * sizeof(float2);
+    const size_t nn = (size_t)n * n, st2 = 2 * nn;
     int rc;
     AD_CUDA(cudaMemsetAsync(w.acc_step, 0, sizeof(double) * (8 * (size_t)K + 3), st));
-    AD_CUDA(cudaMemcpyAsync(w.X, h.P, nn * sizeof(float2), cudaMemcpyDeviceToDevice, st));
-    AD_CUDA(cudaMemcpyAsync(w.X + nn, h.S, nn * sizeof(float2), cudaMemcpyDeviceToDevice, st));
-    // forward: checkpoints every L steps (store_all: X_s, W_s, F_s of every step)
-    for (int s = 0; s < K; ++s) {
-        if (store_all) {
-            const size_t j = (size_t)s * 2 * nn;
-            AD_CUDA(cudaMemcpyAsync(w.Xs + j, w.X, sb, cudaMemcpyDeviceToDevice, st));
-            if ((rc = rk4_state(n, w.X, h, d, s, st))) return rc;
-            if ((rc = diffraction_fwd(n, w.X, w.Fs + j, d, st))) return rc;
-            AD_CUDA(cudaMemcpyAsync(w.Ws + j, w.X, sb, cudaMemcpyDeviceToDevice, st));
-            if ((rc = rk4_state(n, w.X, h, d, s, st))) return rc;
-            continue;
-        }
-        if (s % L == 0) AD_CUDA(cudaMemcpyAsync(w.ck + (size_t)(s / L) * 2 * nn, w.X, sb, cudaMemcpyDeviceToDevice, st));
-        if ((rc = rk4_state(n, w.X, h, d, s, st))) return rc;
-        if ((rc = diffraction_fwd(n, w.X, nullptr, d, st))) return rc;
-        if ((rc = rk4_state(n, w.X, h, d, s, st))) return rc;
+    // forward from the inputs: checkpoints every L steps (store_all: X_s, W_s, F_s of every
+    // step); X_K into w.X
+    for (int s = 0; s <= K; ++s) {
+        const bool fin = s > 0, start = s < K;
+        float2 *w_out = (store_all && fin) ? w.Ws + (size_t)(s - 1) * st2 : nullptr;
+        float2 *x_out = (store_all && start) ? w.Xs + (size_t)s * st2 : nullptr;
+        float2 *ck_out = (!store_all && start && s % L == 0) ? w.ck + (size_t)(s / L) * st2 : nullptr;
+        AD_CUDA(launch_adj_rows_fwd(n, d, w.X, s, fin, start, h.P, h.S, w_out, x_out, ck_out, start ? nullptr : w.X,
+                                    st));
+        if (start) AD_CUDA(launch_colpass(n, 0, w.X, store_all ? w.Fs + (size_t)s * st2 : nullptr, d, nullptr, st));
     }
     AD_CUDA(launch_abs2_sum(w.X + nn, (int)nn, w.acc_glob + 2, st));
     AD_CUDA(launch_seed_cotangent(w.X + nn, w.cot, w.cot + nn, (int)nn, w.acc_glob + 3, st));
-    // backward
+    // backward, segment by segment from the last; the cotangent of X_{s1} enters each
+    // segment in natural layout in w.cot. Boundary s: finish step s+1 (RK4^T at X_{s+1}),
+    // start step s (RK4^T at W_s).
+    auto backward = [&](int s0, int s1, size_t set) -> int {
+        float2 *Xs = w.Xs + set, *Ws = w.Ws + set, *Fs = w.Fs + set;
+        for (int s = s1 - 1; s >= s0 - 1; --s) {
+            const bool fin = s < s1 - 1, start = s >= s0;
+            const float2 *Xn = fin ? Xs + (size_t)(s + 1 - s0) * st2 : nullptr;
+            const float2 *Wn = start ? Ws + (size_t)(s - s0) * st2 : nullptr;
+            double *af = fin ? w.acc_step + 8 * (size_t)(s + 1) : nullptr;
+            double *as = start ? w.acc_step + 8 * (size_t)s : nullptr;
+            AD_CUDA(launch_adj_rows_bwd(n, d, w.cot, s, fin, start, Xn, Wn, af, as, st));
+            if (start) AD_CUDA(launch_colpass(n, 1, w.cot, Fs + (size_t)(s - s0) * st2, d, w.acc_glob, st));
+        }
+        return SHG_OK;
+    };
+    if (store_all) return backward(0, K, 0);
+    // replay of segment seg from its checkpoint on the side branch, keeping X_s, W_s, F_s for
+    // s0 <= s < s1 in slot set seg & 1 (X_{s1} is not needed and lands in w.X)
+    auto replay = [&](int seg) -> int {
+        const int s0 = seg * L, s1 = std::min(K, s0 + L);
+        const size_t set = (size_t)(seg & 1) * L * st2;
+        float2 *Xs = w.Xs + set, *Ws = w.Ws + set, *Fs = w.Fs + set;
+        const float2 *ckp = w.ck + (size_t)seg * st2;
+        for (int s = s0; s <= s1; ++s) {
+            const bool fin = s > s0, start = s < s1;
+            float2 *w_out = fin ? Ws + (size_t)(s - 1 - s0) * st2 : nullptr;
+            float2 *x_out = start ? Xs + (size_t)(s - s0) * st2 : nullptr;
+            AD_CUDA(launch_adj_rows_fwd(n, d, w.X, s, fin, start, ckp, ckp + nn, w_out, x_out, nullptr,
+                                        start ? nullptr : w.X, w.side));
+            if (start) AD_CUDA(launch_colpass(n, 0, w.X, Fs + (size_t)(s - s0) * st2, d, nullptr, w.side));
+        }
+        return SHG_OK;
+    };
+    // branch b waits for everything enqueued so far on branch a
+    auto join = [&](cudaStream_t a, cudaStream_t b) -> int {
+        AD_CUDA(cudaEventRecord(w.ev, a));
+        AD_CUDA(cudaStreamWaitEvent(b, w.ev, 0));
+        return SHG_OK;
+    };
+    if ((rc = join(st, w.side)) || (rc = replay(nseg - 1))) return rc;
     for (int seg = nseg - 1; seg >= 0; --seg) {
-        const int s0 = store_all ? 0 : seg * L, s1 = store_all ? K : std::min(K, s0 + L);
-        if (!store_all) {
-            AD_CUDA(cudaMemcpyAsync(w.X, w.ck + (size_t)seg * 2 * nn, sb, cudaMemcpyDeviceToDevice, st));
-            for (int s = s0; s < s1; ++s) {
-                const size_t j = (size_t)(s - s0) * 2 * nn;
-                AD_CUDA(cudaMemcpyAsync(w.Xs + j, w.X, sb, cudaMemcpyDeviceToDevice, st));
-                if ((rc = rk4_state(n, w.X, h, d, s, st))) return rc;
-                if ((rc = diffraction_fwd(n, w.X, w.Fs + j, d, st))) return rc;
-                AD_CUDA(cudaMemcpyAsync(w.Ws + j, w.X, sb, cudaMemcpyDeviceToDevice, st));
-                if ((rc = rk4_state(n, w.X, h, d, s, st))) return rc;
-            }
-        }
-        for (int s = s1 - 1; s >= s0; --s) {
-            const size_t j = (size_t)(s - s0) * 2 * nn;
-            double *as = w.acc_step + 8 * (size_t)s;
-            AD_CUDA(launch_rk4_vjp(w.Ws + j, w.Ws + j + nn, w.cot, w.cot + nn, (int)nn, h.stepc, s, d, as, st));
-            if ((rc = diffraction_adj(n, w.cot, w.Fs + j, d, w.acc_glob, st))) return rc;
-            AD_CUDA(launch_rk4_vjp(w.Xs + j, w.Xs + j + nn, w.cot, w.cot + nn, (int)nn, h.stepc, s, d, as, st));
-        }
-        if (store_all) break;
+        if ((rc = join(w.side, st))) return rc;  // replay(seg) done
+        // replay(seg-1) reuses the slot set of backward(seg+1), which st has finished
+        if (seg >= 1 && ((rc = join(st, w.side)) || (rc = replay(seg - 1)))) return rc;
+        const int s0 = seg * L, s1 = std::min(K, s0 + L);
+        if ((rc = backward(s0, s1, (size_t)(seg & 1) * L * st2))) return rc;
     }
     return SHG_OK;
 }
@@ -193,6 +195,8 @@ int adjoint_run(const shg_config &cfg, const InstDesc &h, const InstDesc *d, flo
         if (w.graph) cudaGraphExecDestroy(w.graph);
         w.graph = nullptr;
         if (!w.cap) AD_CUDA(cudaStreamCreateWithFlags(&w.cap, cudaStreamNonBlocking));
+        if (!w.side) AD_CUDA(cudaStreamCreateWithFlags(&w.side, cudaStreamNonBlocking));
+        if (!w.ev) AD_CUDA(cudaEventCreateWithFlags(&w.ev, cudaEventDisableTiming));
         cudaGraph_t g = nullptr;
         AD_CUDA(cudaStreamBeginCapture(w.cap, cudaStreamCaptureModeThreadLocal));
         rc = enqueue_pass(h, d, w, L, nseg, store_all, w.cap);

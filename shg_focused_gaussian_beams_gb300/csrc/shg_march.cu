@@ -296,15 +296,16 @@ __global__ void __launch_bounds__(TC * LineShape<N>::G) k_cols(const InstDesc *_
     const int f = blockIdx.y;
     float2 *F = f == 0 ? d.P : d.S;
     const float2 *__restrict__ H = f == 0 ? d.Hp : d.Hs;
+    // propagator values first: their latency overlaps the transform
+    float2 h[E];
+#pragma unroll
+    for (int r = 0; r < E; ++r) h[r] = __ldg(H + (size_t)spec_index<N, G>(t, r) * N + x);
     float2 v[E];
 #pragma unroll
     for (int j = 0; j < E; ++j) v[j] = F[(size_t)(t + G * j) * N + x];
     fft_nat_to_spec<N, G, +1, true, TC, G>(v, t, sc, tab);
 #pragma unroll
-    for (int r = 0; r < E; ++r) {
-        const int k = spec_index<N, G>(t, r);
-        v[r] = c_mul(v[r], __ldg(H + (size_t)k * N + x));
-    }
+    for (int r = 0; r < E; ++r) v[r] = c_mul(v[r], h[r]);
     fft_spec_to_nat<N, G, -1, true, TC, G>(v, t, sc, tab);
 #pragma unroll
     for (int j = 0; j < E; ++j) F[(size_t)(t + G * j) * N + x] = v[j];
