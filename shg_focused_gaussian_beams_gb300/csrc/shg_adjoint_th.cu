@@ -70,7 +70,7 @@ __global__ void k_th_rk4_vjp(const float2 *__restrict__ X0, float2 *cot, const f
     float2 *cP = cot + (size_t)b * 2 * nn, *cS = cP + nn;
     const float4 *__restrict__ cs = coef + ((size_t)b * K + s) * nn;
     const float hp = d.hp, t0 = d.tpa0, w6 = d.dz6;
-    double unused[5];
+    float unused[5];  // parameter sensitivities are not needed here
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += gridDim.x * blockDim.x) {
         const ThCoef k = th_coef_of(cs[i], s, d.dz);
         const float t1 = k.tpa1;

@@ -170,8 +170,12 @@ __device__ __forceinline__ bool heat_voxel(const HeatCoef &c, int x, int y, int 
 // Interior voxel (Tfield.h:132) with the three divisions by dx^2, dy^2, dz^2 taken as
 // corrected products when all three numerators lie in the verified exponent range (one
 // combined test), else through div_const: bit-identical to heat_voxel's interior branch.
+// Biased exponent in [kDivExpLo, kDivExpHi] is |a| in [2^-100, 2^101): two float compares
+// (NaN and infinity fail them, as their exponent 255 fails the range).
+static_assert(kDivExpLo == 27 && kDivExpHi == 227, "div_in_range bounds follow the exponent range");
 __device__ __forceinline__ bool div_in_range(float a) {
-    return ((__float_as_uint(a) & 0x7f800000u) - (kDivExpLo << 23)) <= ((kDivExpHi - kDivExpLo) << 23);
+    const float m = fabsf(a);
+    return m >= 0x1p-100f && m < 0x1p101f;
 }
 
 __device__ __forceinline__ float interior_voxel(const HeatCoef &c, float xm, float xp, float ym, float yp, float zm,
