@@ -53,11 +53,10 @@ __global__ void __launch_bounds__(TC * LineShape<N>::G) k_colpass(float2 *A0, fl
     const int c = threadIdx.x % TC, t = threadIdx.x / TC, x = blockIdx.x * TC + c;
     // propagator values (and the stored spectrum) first: their latency overlaps the transform
     float2 hv[E], fv[MODE == 1 ? E : 1];
+    hprop_load<N>(H, x, t, hv);
+    if constexpr (MODE == 1) {
 #pragma unroll
-    for (int r = 0; r < E; ++r) {
-        const size_t i = (size_t)spec_index<N, G>(t, r) * N + x;
-        hv[r] = __ldg(H + i);
-        if constexpr (MODE == 1) fv[r] = Fst[i];
+        for (int r = 0; r < E; ++r) fv[r] = Fst[(size_t)spec_index<N, G>(t, r) * N + x];
     }
     float2 v[E];
 #pragma unroll

@@ -209,4 +209,43 @@ template <> struct LineShape<128> { static constexpr int G = 8; };
 template <> struct LineShape<256> { static constexpr int G = 16; };
 template <> struct LineShape<512> { static constexpr int G = 16; };
 
+// Propagator storage order. The column transforms (G = LineShape<N>::G threads per column,
+// E = N / G registers each) multiply register r of thread t by the propagator of spectral
+// row k = spec_index<N, G>(t, r) and column x. Registers r = 2j, 2j+1 of thread t form one
+// 16-byte word, and the words of consecutive columns are adjacent: word (t * E/2 + j) * N + x.
+// A warp over consecutive columns then reads whole segments with E/2 loads per thread
+// instead of E.
+__host__ __device__ inline int line_threads(int n) { return n <= 32 ? 4 : (n <= 128 ? 8 : 16); }
+
+__host__ __device__ inline size_t hprop_index_rt(int n, int k, int x) {
+    const int G = line_threads(n), E = n / G, Q = E / G;
+    const int rem = k % E, k1 = k / E;
+    const int t = rem / Q, r = (rem % Q) * G + k1;
+    return (((size_t)t * (E / 2) + (r >> 1)) * n + x) * 2 + (r & 1);
+}
+
+template <int N>
+__device__ __forceinline__ size_t hprop_index(int k, int x) {
+    constexpr int G = LineShape<N>::G, E = N / G, Q = E / G;
+    const int rem = k % E, k1 = k / E;
+    const int t = rem / Q, r = (rem % Q) * G + k1;
+    return (((size_t)t * (E / 2) + (r >> 1)) * N + x) * 2 + (r & 1);
+}
+
+// The E propagator values of column x for thread t of a column transform with
+// G = LineShape<N>::G (H 16-byte aligned).
+template <int N>
+__device__ __forceinline__ void hprop_load(const float2 *__restrict__ H, int x, int t,
+                                           float2 (&h)[N / LineShape<N>::G]) {
+    constexpr int G = LineShape<N>::G, E = N / G;
+    static_assert(E % 2 == 0, "pairs of values per 16-byte load");
+    const float4 *p = reinterpret_cast<const float4 *>(H);
+#pragma unroll
+    for (int j = 0; j < E / 2; ++j) {
+        const float4 q = __ldg(p + ((size_t)t * (E / 2) + j) * N + x);
+        h[2 * j] = make_float2(q.x, q.y);
+        h[2 * j + 1] = make_float2(q.z, q.w);
+    }
+}
+
 }  // namespace shg

@@ -102,8 +102,10 @@ __global__ void k_setup_fields(const InstDesc *__restrict__ inst) {
         float s1, c1, s2, c2;
         sincosf(php, &s1, &c1);
         sincosf(phs, &s2, &c2);
-        d.Hp[i] = make_float2(c1 * d.inv_nn, s1 * d.inv_nn);
-        d.Hs[i] = make_float2(c2 * d.inv_nn, s2 * d.inv_nn);
+        // stored in the column transforms' order (hprop_index_rt, shg_fft.cuh)
+        const size_t ih = hprop_index_rt(n, iy, ix);
+        d.Hp[ih] = make_float2(c1 * d.inv_nn, s1 * d.inv_nn);
+        d.Hs[ih] = make_float2(c2 * d.inv_nn, s2 * d.inv_nn);
     }
     block_add_double(acc, d.acc + 0);
 }
@@ -298,8 +300,7 @@ __global__ void __launch_bounds__(TC * LineShape<N>::G) k_cols(const InstDesc *_
     const float2 *__restrict__ H = f == 0 ? d.Hp : d.Hs;
     // propagator values first: their latency overlaps the transform
     float2 h[E];
-#pragma unroll
-    for (int r = 0; r < E; ++r) h[r] = __ldg(H + (size_t)spec_index<N, G>(t, r) * N + x);
+    hprop_load<N>(H, x, t, h);
     float2 v[E];
 #pragma unroll
     for (int j = 0; j < E; ++j) v[j] = F[(size_t)(t + G * j) * N + x];

@@ -174,8 +174,12 @@ __global__ void __launch_bounds__(ResShape<N, CS_, MINB_, G_>::THREADS, MINB_)
                     };
                     // propagator values first: their L2 latency overlaps the column transform
                     float2 h[E];
+                    if constexpr (G == LineShape<N>::G) {
+                        hprop_load<N>(H, x, ct, h);
+                    } else {
 #pragma unroll
-                    for (int r = 0; r < E; ++r) h[r] = __ldg(H + (size_t)spec_index<N, G>(ct, r) * N + x);
+                        for (int r = 0; r < E; ++r) h[r] = __ldg(H + hprop_index<N>(spec_index<N, G>(ct, r), x));
+                    }
                     float2 v[E];
 #pragma unroll
                     for (int j = 0; j < E; ++j) v[j] = *at(j);
