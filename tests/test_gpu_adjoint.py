@@ -125,6 +125,29 @@ def test_gradient_field_vs_torch_fp64_reference(case):
     assert rel < FD_RTOL, rel
 
 
+@pytest.mark.parametrize("n", [16, 32, 128])
+def test_gradient_field_every_grid_size(n):
+    """The fused adjoint row and column passes at the grid sizes the 64^2 and 256^2 cases do
+    not reach: the whole pump-gradient field (12 slices, 3 checkpoints) against torch
+    autograd through the complex128 restatement."""
+    nz = 12
+    inst = W.plain_instance(n, nz, P0, 2.84, T0)
+    cfg = O.make_cfg(W.CRYSTAL_QPM50, n, n, nz, inst.lx, inst.ly)
+    o = O.Oracle(cfg)
+    rng = np.random.default_rng(n)
+    pump64 = o.set_pump64(inst.power, inst.focal, inst.waist, T0) * (1 + 0.05 * smooth_noise(rng, n, cells=2))
+    c = dict(cfg=cfg, o=o, dk32=float(o.dk_constant(T0)))
+    s = Solver(crystal=W.CRYSTAL_QPM50, nx=n, ny=n, nz=nz, lx=inst.lx, ly=inst.ly)
+    r = s.grad(T0, torch.from_numpy(pump64.astype(np.complex64)).cuda(), checkpoints=3)
+    p = torch.from_numpy(pump64).cuda().requires_grad_(True)
+    L = torch_loss64(c, p)
+    L.backward()
+    ref = p.grad.cpu().numpy()
+    got = r["grad_pump"].cpu().numpy().astype(np.complex128)
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < FD_RTOL
+    assert abs(r["loss"] - L.item()) / L.item() < 1e-4
+
+
 def test_loss_matches_fp64(case):
     L = loss64(case, case["pump64"])
     assert abs(case["r"]["loss"] - L) / L < 1e-4

@@ -74,6 +74,30 @@ def test_cwes_from_given_fields_matches_oracle(name):
     assert rel_l2(po, po_r) < FIELD_RTOL
 
 
+@pytest.mark.parametrize("march", ["auto", "streaming"])
+@pytest.mark.parametrize("n", [16, 32, 64, 128, 256])
+def test_lone_solve_every_grid_size_vs_oracle(n, march, monkeypatch):
+    """A lone streaming solve runs the one-thread-per-point row pass and the narrow-tile
+    column pass; every compiled grid size, with the schedule the autotuner picks and with
+    the streaming passes forced, against the oracle's FP32 restatement (perturbed fields,
+    SH seeded, 12 slices)."""
+    monkeypatch.setenv("SHG_MARCH", march)
+    inst = W.plain_instance(n, 12, 20.0, 2.84, 50.0)
+    o = O.Oracle(O.make_cfg(W.CRYSTAL_QPM50, n, n, 12, inst.lx, inst.ly))
+    rng = np.random.default_rng(n)
+    pump = o.set_pump(inst.power, inst.focal, inst.waist, inst.temp)
+    pump = (pump * (1 + 0.05 * (rng.standard_normal(pump.shape) + 1j * rng.standard_normal(pump.shape))))
+    pump = pump.astype(np.complex64)
+    sh = (0.01 * pump * np.exp(1j * rng.uniform(0, 6.28, pump.shape))).astype(np.complex64)
+    po_r, so_r, _, _ = o.cwes_plain(pump, sh, inst.temp)
+    s = Solver(crystal=W.CRYSTAL_QPM50, nx=n, ny=n, nz=12, lx=inst.lx, ly=inst.ly)
+    s.set_input_fields(pump, sh)
+    s.cwes(inst.temp)
+    po, so = s.fields()
+    assert rel_l2(so, so_r) < FIELD_RTOL
+    assert rel_l2(po, po_r) < FIELD_RTOL
+
+
 def test_device_pointer_cwes_matches_host_api():
     g = golden("c0_small.npz")
     s = _solver_for(g)
