@@ -9,7 +9,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 
-# Parity bar (the benchmark spec): output fields within relative L2 1e-4 and conversion
+# Parity bar: output fields within relative L2 1e-4 and conversion
 # efficiency within 1e-4 relative of the reference's FP32 build and of the FP64 run.
 FIELD_RTOL = 1e-4
 ETA_RTOL = 1e-4
