@@ -24,6 +24,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -557,8 +558,22 @@ def run_ours(args):
         issue = {"achieved": inst_s, "peak": peak_inst, "unit": "thread-instructions/s", "frac": inst_s / peak_inst,
                  "thread_inst_per_pt_step": tr["thread_inst_per_pt_step"], "source": tr.get("inst_source"),
                  "peak_note": f"{props.multi_processor_count} SMs x 128 lanes x {sm_mhz:.0f} MHz (nominal issue rate)"}
+    fp32 = None
+    if dom.startswith("resident<"):  # the whole step in one kernel
+        # flops of the method per grid-pt.z-step: 4 2D FFTs at 5 N log2 N, 2 propagator
+        # products, 2 RK4 calls (20 log2(N^2) + 456; sincos not counted), against the nominal
+        # FP32 rate (no measured FP32 peak exists): SMs x 128 lanes x 2 flop x SM clock
+        props = torch.cuda.get_device_properties(local)
+        n_dom = int(dom[dom.index("<") + 1:-1])
+        flop_pt = 20.0 * math.log2(n_dom * n_dom) + 456.0
+        pt_steps = bytes_k / n_l / 32.0
+        fl_s = flop_pt * pt_steps / (ms_k / n_l * 1e-3)
+        sm_mhz = clk.summary().get("sm_mhz") or 2070.0
+        peak_fl = props.multi_processor_count * 128 * 2 * sm_mhz * 1e6
+        fp32 = {"achieved": fl_s / 1e12, "peak": peak_fl / 1e12, "unit": "TFLOP/s", "frac": fl_s / peak_fl,
+                "flop_per_pt_step": flop_pt, "peak_note": "nominal FP32 rate at the sampled SM clock"}
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_source": peak_kind, "launches": n_l, "issue": issue,
+            "frac": achieved / peak, "peak_source": peak_kind, "launches": n_l, "issue": issue, "fp32": fp32,
             "ms_per_launch": ms_k / n_l, "algorithmic_bytes_per_launch": bytes_k / n_l,
             "traffic": traffic,
             "traffic_source": None if tr is None else tr.get("source"),
