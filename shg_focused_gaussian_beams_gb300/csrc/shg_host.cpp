@@ -506,13 +506,14 @@ class Batch {
 
     // Second stage: the classes share the GPU in a run (one stream each), so the fastest
     // schedule of a class alone is not always the fastest beside the others. For each class
-    // the two fastest schedules alone are tried, timing the whole concurrent run of every
-    // combination as a captured graph (second of two launches). Cached per device and batch
-    // shape.
+    // the two fastest schedules alone (and the streaming passes for classes of one to three
+    // solves) are tried, timing the whole concurrent run of every combination as a captured
+    // graph (second of two launches). Also run for a single class, whose first-stage times
+    // come from direct launches. Cached per device and batch shape.
     int tune_mix(cudaStream_t st, cudaEvent_t a, cudaEvent_t b) {
         const int nc = (int)classes_.size();
         mix_.clear();
-        if (nc < 2) return SHG_OK;
+        if (nc < 1) return SHG_OK;
         std::vector<int> order(nc);
         for (int i = 0; i < nc; ++i) order[i] = i;
         std::sort(order.begin(), order.end(), [&](int x, int y) { return classes_[x].n > classes_[y].n; });
@@ -553,6 +554,12 @@ class Batch {
             if (t.empty()) return SHG_OK;  // schedule fixed by the caller: keep it
             std::sort(t.begin(), t.end(), [](const Trial &x, const Trial &y) { return x.ms < y.ms; });
             for (int k = 0; k < (int)t.size() && k < 2; ++k) opts[oi].push_back({t[k].resident, t[k].v});
+            // a class of one to three solves: the first stage times direct launches, where
+            // the streaming passes (two small launches per step) pay the host's launch cost
+            // that a captured graph does not, so they are always timed here as well
+            bool has_streaming = false;
+            for (const Pick &p : opts[oi]) has_streaming |= !p.resident;
+            if (classes_[order[oi]].count < 4 && !has_streaming) opts[oi].push_back({false, {0, 0, 0}});
             ncomb *= (int)opts[oi].size();
         }
         float best = 1e30f;
