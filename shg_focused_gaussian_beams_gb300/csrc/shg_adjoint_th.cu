@@ -60,6 +60,52 @@ __global__ void k_th_rk4_state(float2 *X, float2 *save, const float4 *__restrict
     }
 }
 
+// RK4_th^T of one point at the base state (P, S) with stage constants k: (cp, cs) hold the
+// cotangent of the RK4 output on entry and of its input on exit (stages 1..4 use the
+// constants c0, c1, c1, c2).
+__device__ __forceinline__ void th_vjp_point(const float2 P, const float2 S, float2 &cp, float2 &cs, const ThCoef &k,
+                                             float hp, float t0, float w6) {
+    const float t1 = k.tpa1;
+    float unused[5];  // parameter sensitivities are not needed here
+    float2 k1p, k1s, k2p, k2s, k3p, k3s;
+    dadz_point(P, S, k.c0, hp, t0, t1, k1p, k1s);
+    const float2 B2p = make_float2(fmaf(0.5f, k1p.x, P.x), fmaf(0.5f, k1p.y, P.y));
+    const float2 B2s = make_float2(fmaf(0.5f, k1s.x, S.x), fmaf(0.5f, k1s.y, S.y));
+    dadz_point(B2p, B2s, k.c1, hp, t0, t1, k2p, k2s);
+    const float2 B3p = make_float2(fmaf(0.5f, k2p.x, P.x), fmaf(0.5f, k2p.y, P.y));
+    const float2 B3s = make_float2(fmaf(0.5f, k2s.x, S.x), fmaf(0.5f, k2s.y, S.y));
+    dadz_point(B3p, B3s, k.c1, hp, t0, t1, k3p, k3s);
+    const float2 B4p = c_add(P, k3p), B4s = c_add(S, k3s);
+    const float2 op = cp, os = cs;
+    float2 cap = op, cas = os;
+    float2 ck3p = make_float2(2.0f * w6 * op.x, 2.0f * w6 * op.y), ck3s = make_float2(2.0f * w6 * os.x, 2.0f * w6 * os.y);
+    float2 ck2p = ck3p, ck2s = ck3s;
+    float2 ck1p = make_float2(w6 * op.x, w6 * op.y), ck1s = make_float2(w6 * os.x, w6 * os.y);
+    const float2 ck4p = ck1p, ck4s = ck1s;
+    float2 bp = make_float2(0.f, 0.f), bs = make_float2(0.f, 0.f);
+    dadz_vjp(B4p, B4s, ck4p, ck4s, k.c2, hp, t0, t1, bp, bs, unused);
+    cap = c_add(cap, bp);
+    cas = c_add(cas, bs);
+    ck3p = c_add(ck3p, bp);
+    ck3s = c_add(ck3s, bs);
+    bp = bs = make_float2(0.f, 0.f);
+    dadz_vjp(B3p, B3s, ck3p, ck3s, k.c1, hp, t0, t1, bp, bs, unused);
+    cap = c_add(cap, bp);
+    cas = c_add(cas, bs);
+    ck2p = make_float2(fmaf(0.5f, bp.x, ck2p.x), fmaf(0.5f, bp.y, ck2p.y));
+    ck2s = make_float2(fmaf(0.5f, bs.x, ck2s.x), fmaf(0.5f, bs.y, ck2s.y));
+    bp = bs = make_float2(0.f, 0.f);
+    dadz_vjp(B2p, B2s, ck2p, ck2s, k.c1, hp, t0, t1, bp, bs, unused);
+    cap = c_add(cap, bp);
+    cas = c_add(cas, bs);
+    ck1p = make_float2(fmaf(0.5f, bp.x, ck1p.x), fmaf(0.5f, bp.y, ck1p.y));
+    ck1s = make_float2(fmaf(0.5f, bs.x, ck1s.x), fmaf(0.5f, bs.y, ck1s.y));
+    bp = bs = make_float2(0.f, 0.f);
+    dadz_vjp(P, S, ck1p, ck1s, k.c0, hp, t0, t1, bp, bs, unused);
+    cp = c_add(cap, bp);
+    cs = c_add(cas, bs);
+}
+
 // RK4_th^T of step s at the base states X0: cot holds the cotangent of the RK4 output on
 // entry and of its input on exit (stages 1..4 use the constants c0, c1, c1, c2).
 __global__ void k_th_rk4_vjp(const float2 *__restrict__ X0, float2 *cot, const float4 *__restrict__ coef, int nn,
@@ -70,48 +116,65 @@ __global__ void k_th_rk4_vjp(const float2 *__restrict__ X0, float2 *cot, const f
     float2 *cP = cot + (size_t)b * 2 * nn, *cS = cP + nn;
     const float4 *__restrict__ cs = coef + ((size_t)b * K + s) * nn;
     const float hp = d.hp, t0 = d.tpa0, w6 = d.dz6;
-    float unused[5];  // parameter sensitivities are not needed here
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += gridDim.x * blockDim.x) {
         const ThCoef k = th_coef_of(cs[i], s, d.dz);
-        const float t1 = k.tpa1;
-        const float2 P = P0[i], S = S0[i];
-        float2 k1p, k1s, k2p, k2s, k3p, k3s;
-        dadz_point(P, S, k.c0, hp, t0, t1, k1p, k1s);
-        const float2 B2p = make_float2(fmaf(0.5f, k1p.x, P.x), fmaf(0.5f, k1p.y, P.y));
-        const float2 B2s = make_float2(fmaf(0.5f, k1s.x, S.x), fmaf(0.5f, k1s.y, S.y));
-        dadz_point(B2p, B2s, k.c1, hp, t0, t1, k2p, k2s);
-        const float2 B3p = make_float2(fmaf(0.5f, k2p.x, P.x), fmaf(0.5f, k2p.y, P.y));
-        const float2 B3s = make_float2(fmaf(0.5f, k2s.x, S.x), fmaf(0.5f, k2s.y, S.y));
-        dadz_point(B3p, B3s, k.c1, hp, t0, t1, k3p, k3s);
-        const float2 B4p = c_add(P, k3p), B4s = c_add(S, k3s);
-        const float2 op = cP[i], os = cS[i];
-        float2 cap = op, cas = os;
-        float2 ck3p = make_float2(2.0f * w6 * op.x, 2.0f * w6 * op.y), ck3s = make_float2(2.0f * w6 * os.x, 2.0f * w6 * os.y);
-        float2 ck2p = ck3p, ck2s = ck3s;
-        float2 ck1p = make_float2(w6 * op.x, w6 * op.y), ck1s = make_float2(w6 * os.x, w6 * os.y);
-        const float2 ck4p = ck1p, ck4s = ck1s;
-        float2 bp = make_float2(0.f, 0.f), bs = make_float2(0.f, 0.f);
-        dadz_vjp(B4p, B4s, ck4p, ck4s, k.c2, hp, t0, t1, bp, bs, unused);
-        cap = c_add(cap, bp);
-        cas = c_add(cas, bs);
-        ck3p = c_add(ck3p, bp);
-        ck3s = c_add(ck3s, bs);
-        bp = bs = make_float2(0.f, 0.f);
-        dadz_vjp(B3p, B3s, ck3p, ck3s, k.c1, hp, t0, t1, bp, bs, unused);
-        cap = c_add(cap, bp);
-        cas = c_add(cas, bs);
-        ck2p = make_float2(fmaf(0.5f, bp.x, ck2p.x), fmaf(0.5f, bp.y, ck2p.y));
-        ck2s = make_float2(fmaf(0.5f, bs.x, ck2s.x), fmaf(0.5f, bs.y, ck2s.y));
-        bp = bs = make_float2(0.f, 0.f);
-        dadz_vjp(B2p, B2s, ck2p, ck2s, k.c1, hp, t0, t1, bp, bs, unused);
-        cap = c_add(cap, bp);
-        cas = c_add(cas, bs);
-        ck1p = make_float2(fmaf(0.5f, bp.x, ck1p.x), fmaf(0.5f, bp.y, ck1p.y));
-        ck1s = make_float2(fmaf(0.5f, bs.x, ck1s.x), fmaf(0.5f, bs.y, ck1s.y));
-        bp = bs = make_float2(0.f, 0.f);
-        dadz_vjp(P, S, ck1p, ck1s, k.c0, hp, t0, t1, bp, bs, unused);
-        cP[i] = c_add(cap, bp);
-        cS[i] = c_add(cas, bs);
+        float2 a = cP[i], c = cS[i];
+        th_vjp_point(P0[i], S0[i], a, c, k, hp, t0, w6);
+        cP[i] = a;
+        cS[i] = c;
+    }
+}
+
+// Step boundary of the forward march in one pass over every solve's state X: RK4_th of step
+// sp (its second call, slice sp; skipped for sp < 0) with its input stored to save_w, then
+// the state stored to save_x, then RK4_th of step sn (its first call, slice sn; skipped for
+// sn < 0). Replaces two k_th_rk4_state passes, so the state crosses memory once.
+__global__ void k_th_rk4_pair(float2 *X, float2 *save_w, float2 *save_x, const float4 *__restrict__ coef, int nn,
+                              int K, int sp, int sn, const InstDesc *__restrict__ dd) {
+    const int b = blockIdx.y;
+    const InstDesc &d = dd[b];
+    float2 *P = X + (size_t)b * 2 * nn, *S = P + nn;
+    const size_t o = (size_t)b * 2 * nn;
+    const float4 *__restrict__ cp = coef + ((size_t)b * K + (sp < 0 ? 0 : sp)) * nn;
+    const float4 *__restrict__ cn = coef + ((size_t)b * K + (sn < 0 ? 0 : sn)) * nn;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += gridDim.x * blockDim.x) {
+        float2 p = P[i], q = S[i];
+        if (sp >= 0) {
+            if (save_w) {
+                save_w[o + i] = p;
+                save_w[o + nn + i] = q;
+            }
+            rk4_point_th(p, q, th_coef_of(cp[i], sp, d.dz), d);
+        }
+        if (save_x) {
+            save_x[o + i] = p;
+            save_x[o + nn + i] = q;
+        }
+        if (sn >= 0) rk4_point_th(p, q, th_coef_of(cn[i], sn, d.dz), d);
+        P[i] = p;
+        S[i] = q;
+    }
+}
+
+// Step boundary of the reverse sweep in one pass over every solve's cotangent: RK4_th^T of
+// step sa at its first call's input Xa (skipped for sa < 0), then RK4_th^T of step sb at its
+// second call's input Wb (skipped for sb < 0).
+__global__ void k_th_vjp_pair(const float2 *__restrict__ Xa, const float2 *__restrict__ Wb, float2 *cot,
+                              const float4 *__restrict__ coef, int nn, int K, int sa, int sb,
+                              const InstDesc *__restrict__ dd) {
+    const int b = blockIdx.y;
+    const InstDesc &d = dd[b];
+    const size_t o = (size_t)b * 2 * nn;
+    float2 *cP = cot + o, *cS = cP + nn;
+    const float4 *__restrict__ ca = coef + ((size_t)b * K + (sa < 0 ? 0 : sa)) * nn;
+    const float4 *__restrict__ cb = coef + ((size_t)b * K + (sb < 0 ? 0 : sb)) * nn;
+    const float hp = d.hp, t0 = d.tpa0, w6 = d.dz6;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += gridDim.x * blockDim.x) {
+        float2 a = cP[i], c = cS[i];
+        if (sa >= 0) th_vjp_point(Xa[o + i], Xa[o + nn + i], a, c, th_coef_of(ca[i], sa, d.dz), hp, t0, w6);
+        if (sb >= 0) th_vjp_point(Wb[o + i], Wb[o + nn + i], a, c, th_coef_of(cb[i], sb, d.dz), hp, t0, w6);
+        cP[i] = a;
+        cS[i] = c;
     }
 }
 
@@ -154,6 +217,20 @@ cudaError_t launch_th_rk4_state(float2 *X, float2 *save, const float4 *coef, int
 cudaError_t launch_th_rk4_vjp(const float2 *X0, float2 *cot, const float4 *coef, int nn, int K, int s,
                               const InstDesc *d, int solves, cudaStream_t st) {
     k_th_rk4_vjp<<<grid_b(nn, solves), 256, 0, st>>>(X0, cot, coef, nn, K, s, d);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_th_rk4_pair(float2 *X, float2 *save_w, float2 *save_x, const float4 *coef, int nn, int K, int sp,
+                               int sn, const InstDesc *d, int solves, cudaStream_t st) {
+    if (sp >= K || sn >= K) return cudaErrorInvalidValue;
+    k_th_rk4_pair<<<grid_b(nn, solves), 256, 0, st>>>(X, save_w, save_x, coef, nn, K, sp, sn, d);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_th_vjp_pair(const float2 *Xa, const float2 *Wb, float2 *cot, const float4 *coef, int nn, int K,
+                               int sa, int sb, const InstDesc *d, int solves, cudaStream_t st) {
+    if (sa >= K || sb >= K || (sa >= 0 && !Xa) || (sb >= 0 && !Wb)) return cudaErrorInvalidValue;
+    k_th_vjp_pair<<<grid_b(nn, solves), 256, 0, st>>>(Xa, Wb, cot, coef, nn, K, sa, sb, d);
     return cudaGetLastError();
 }
 

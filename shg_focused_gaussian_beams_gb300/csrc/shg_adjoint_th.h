@@ -21,6 +21,13 @@ cudaError_t launch_th_rk4_state(float2 *X, float2 *save, const float4 *coef, int
                                 int solves, cudaStream_t st);
 cudaError_t launch_th_rk4_vjp(const float2 *X0, float2 *cot, const float4 *coef, int nn, int K, int s,
                               const InstDesc *d, int solves, cudaStream_t st);
+// Fused step boundaries: forward RK4 of step sp (second call; input saved to save_w), state
+// saved to save_x, RK4 of step sn (first call); reverse RK4^T of step sa at Xa then of step
+// sb at Wb. A negative step index skips that half.
+cudaError_t launch_th_rk4_pair(float2 *X, float2 *save_w, float2 *save_x, const float4 *coef, int nn, int K, int sp,
+                               int sn, const InstDesc *d, int solves, cudaStream_t st);
+cudaError_t launch_th_vjp_pair(const float2 *Xa, const float2 *Wb, float2 *cot, const float4 *coef, int nn, int K,
+                               int sa, int sb, const InstDesc *d, int solves, cudaStream_t st);
 cudaError_t launch_abs2_sum_b(const float2 *X, int nn, int off, double *out, int solves, cudaStream_t st);
 cudaError_t launch_seed_b(const float2 *X, float2 *cot, int nn, const double *seed, int solves, cudaStream_t st);
 

@@ -211,11 +211,6 @@ int ThermalGradBatch::enqueue(bool grad, int L, int nseg, bool store_all, cudaSt
     TG_CUDA(cudaMemset2DAsync(X_ + nn_, 2 * nn_ * sizeof(float2), 0, nn_ * sizeof(float2), B, st));
     TG_CUDA(launch_abs2_sum_b(X_, nn, 0, sums_ + B, B, st));
     ++nl;
-    auto rk4 = [&](float2 *save, int s) -> int {
-        TG_CUDA(launch_th_rk4_state(X_, save, coef_, nn, K, s, d_desc_, B, st));
-        ++nl;
-        return SHG_OK;
-    };
     auto diffraction = [&](float2 *A, int mode) -> int {
         TG_CUDA(launch_dft_rows(n, +1, A, A, st, 2 * B));
         TG_CUDA(launch_colpass(n, mode, A, nullptr, d_desc_, nullptr, st, B));
@@ -223,16 +218,23 @@ int ThermalGradBatch::enqueue(bool grad, int L, int nseg, bool store_all, cudaSt
         nl += 3;
         return SHG_OK;
     };
+    // Step boundary s (0 <= s <= K) of the forward march on X_: second RK4 of step s-1
+    // (input W_{s-1} to save_w), X_s to save_x, first RK4 of step s; one pass per boundary.
+    auto boundary = [&](int s, int s_end, float2 *save_w, float2 *save_x) -> int {
+        TG_CUDA(launch_th_rk4_pair(X_, save_w, save_x, coef_, nn, K, s - 1, s < s_end ? s : -1, d_desc_, B, st));
+        ++nl;
+        return SHG_OK;
+    };
+    // forward from the inputs: checkpoints every L steps (store_all: X_s, W_s of every step)
+    auto save_x = [&](int s) -> float2 * {
+        if (!grad || s >= K) return nullptr;
+        if (store_all) return Xs_ + (size_t)s * sz;
+        return s % L == 0 ? ck_ + (size_t)(s / L) * sz : nullptr;
+    };
+    TG_TRY(boundary(0, K, nullptr, save_x(0)));
     for (int s = 0; s < K; ++s) {
-        if (grad && store_all) {
-            TG_TRY(rk4(Xs_ + (size_t)s * sz, s));
-            TG_TRY(diffraction(X_, 0));
-            TG_TRY(rk4(Ws_ + (size_t)s * sz, s));
-            continue;
-        }
-        TG_TRY(rk4(grad && s % L == 0 ? ck_ + (size_t)(s / L) * sz : nullptr, s));
         TG_TRY(diffraction(X_, 0));
-        TG_TRY(rk4(nullptr, s));
+        TG_TRY(boundary(s + 1, K, grad && store_all ? Ws_ + (size_t)s * sz : nullptr, save_x(s + 1)));
     }
     TG_CUDA(launch_abs2_sum_b(X_, nn, nn, sums_, B, st));
     ++nl;
@@ -242,20 +244,28 @@ int ThermalGradBatch::enqueue(bool grad, int L, int nseg, bool store_all, cudaSt
     for (int seg = nseg - 1; seg >= 0; --seg) {
         const int s0 = store_all ? 0 : seg * L, s1 = store_all ? K : std::min(K, s0 + L);
         if (!store_all) {
+            // replay the segment from its checkpoint, keeping X_s, W_s for s0 <= s < s1
             TG_CUDA(cudaMemcpyAsync(X_, ck_ + (size_t)seg * sz, sz * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+            TG_CUDA(launch_th_rk4_pair(X_, nullptr, Xs_, coef_, nn, K, -1, s0, d_desc_, B, st));
+            ++nl;
             for (int s = s0; s < s1; ++s) {
-                const size_t j = (size_t)(s - s0) * sz;
-                TG_TRY(rk4(Xs_ + j, s));
                 TG_TRY(diffraction(X_, 0));
-                TG_TRY(rk4(Ws_ + j, s));
+                const size_t j = (size_t)(s - s0) * sz;
+                TG_TRY(boundary(s + 1, s1, Ws_ + j, s + 1 < s1 ? Xs_ + j + sz : nullptr));
             }
         }
+        // reverse: RK4^T at W_{s1-1}; then per step s the adjoint diffraction and one pass
+        // with RK4^T at X_s and at W_{s-1}
+        TG_CUDA(launch_th_vjp_pair(nullptr, Ws_ + (size_t)(s1 - 1 - s0) * sz, cot_, coef_, nn, K, -1, s1 - 1, d_desc_,
+                                   B, st));
+        ++nl;
         for (int s = s1 - 1; s >= s0; --s) {
-            const size_t j = (size_t)(s - s0) * sz;
-            TG_CUDA(launch_th_rk4_vjp(Ws_ + j, cot_, coef_, nn, K, s, d_desc_, B, st));
             TG_TRY(diffraction(cot_, 2));
-            TG_CUDA(launch_th_rk4_vjp(Xs_ + j, cot_, coef_, nn, K, s, d_desc_, B, st));
-            nl += 2;
+            const size_t j = (size_t)(s - s0) * sz;
+            const bool more = s - 1 >= s0;
+            TG_CUDA(launch_th_vjp_pair(Xs_ + j, more ? Ws_ + j - sz : nullptr, cot_, coef_, nn, K, s, more ? s - 1 : -1,
+                                       d_desc_, B, st));
+            ++nl;
         }
         if (store_all) break;
     }
