@@ -38,28 +38,6 @@ __device__ __forceinline__ ThCoef th_coef_of(float4 cf, int s, float dz) {
     return th_coef_k(cf.x, cf.y, cf.z, cf.w, s, dz);
 }
 
-// Forward RK4_th of step s on every solve's state; the input state is also stored to
-// `save` (same layout) when save != nullptr.
-__global__ void k_th_rk4_state(float2 *X, float2 *save, const float4 *__restrict__ coef, int nn, int K, int s,
-                               const InstDesc *__restrict__ dd) {
-    const int b = blockIdx.y;
-    const InstDesc &d = dd[b];
-    float2 *P = X + (size_t)b * 2 * nn, *S = P + nn;
-    float2 *sv = save ? save + (size_t)b * 2 * nn : nullptr;
-    const float4 *__restrict__ cs = coef + ((size_t)b * K + s) * nn;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += gridDim.x * blockDim.x) {
-        const ThCoef k = th_coef_of(cs[i], s, d.dz);
-        float2 p = P[i], q = S[i];
-        if (sv) {
-            sv[i] = p;
-            sv[nn + i] = q;
-        }
-        rk4_point_th(p, q, k, d);
-        P[i] = p;
-        S[i] = q;
-    }
-}
-
 // RK4_th^T of one point at the base state (P, S) with stage constants k: (cp, cs) hold the
 // cotangent of the RK4 output on entry and of its input on exit (stages 1..4 use the
 // constants c0, c1, c1, c2).
@@ -106,29 +84,10 @@ __device__ __forceinline__ void th_vjp_point(const float2 P, const float2 S, flo
     cs = c_add(cas, bs);
 }
 
-// RK4_th^T of step s at the base states X0: cot holds the cotangent of the RK4 output on
-// entry and of its input on exit (stages 1..4 use the constants c0, c1, c1, c2).
-__global__ void k_th_rk4_vjp(const float2 *__restrict__ X0, float2 *cot, const float4 *__restrict__ coef, int nn,
-                             int K, int s, const InstDesc *__restrict__ dd) {
-    const int b = blockIdx.y;
-    const InstDesc &d = dd[b];
-    const float2 *P0 = X0 + (size_t)b * 2 * nn, *S0 = P0 + nn;
-    float2 *cP = cot + (size_t)b * 2 * nn, *cS = cP + nn;
-    const float4 *__restrict__ cs = coef + ((size_t)b * K + s) * nn;
-    const float hp = d.hp, t0 = d.tpa0, w6 = d.dz6;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += gridDim.x * blockDim.x) {
-        const ThCoef k = th_coef_of(cs[i], s, d.dz);
-        float2 a = cP[i], c = cS[i];
-        th_vjp_point(P0[i], S0[i], a, c, k, hp, t0, w6);
-        cP[i] = a;
-        cS[i] = c;
-    }
-}
-
 // Step boundary of the forward march in one pass over every solve's state X: RK4_th of step
 // sp (its second call, slice sp; skipped for sp < 0) with its input stored to save_w, then
 // the state stored to save_x, then RK4_th of step sn (its first call, slice sn; skipped for
-// sn < 0). Replaces two k_th_rk4_state passes, so the state crosses memory once.
+// sn < 0): the state crosses memory once per step boundary.
 __global__ void k_th_rk4_pair(float2 *X, float2 *save_w, float2 *save_x, const float4 *__restrict__ coef, int nn,
                               int K, int sp, int sn, const InstDesc *__restrict__ dd) {
     const int b = blockIdx.y;
@@ -205,18 +164,6 @@ static dim3 grid_b(int nn, int solves) { return dim3((unsigned)((nn + 255) / 256
 cudaError_t launch_th_coef_table(const float *NP, const float *NS, const float *DK, float4 *coef, int nn, int K,
                                  const ThermDesc &th, cudaStream_t st) {
     k_th_coef_table<<<(nn + 255) / 256, 256, 0, st>>>(NP, NS, DK, coef, nn, K, th);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_th_rk4_state(float2 *X, float2 *save, const float4 *coef, int nn, int K, int s, const InstDesc *d,
-                                int solves, cudaStream_t st) {
-    k_th_rk4_state<<<grid_b(nn, solves), 256, 0, st>>>(X, save, coef, nn, K, s, d);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_th_rk4_vjp(const float2 *X0, float2 *cot, const float4 *coef, int nn, int K, int s,
-                              const InstDesc *d, int solves, cudaStream_t st) {
-    k_th_rk4_vjp<<<grid_b(nn, solves), 256, 0, st>>>(X0, cot, coef, nn, K, s, d);
     return cudaGetLastError();
 }
 

@@ -17,10 +17,6 @@ class ThermalSolve;
 
 cudaError_t launch_th_coef_table(const float *NP, const float *NS, const float *DK, float4 *coef, int nn, int K,
                                  const ThermDesc &th, cudaStream_t st);
-cudaError_t launch_th_rk4_state(float2 *X, float2 *save, const float4 *coef, int nn, int K, int s, const InstDesc *d,
-                                int solves, cudaStream_t st);
-cudaError_t launch_th_rk4_vjp(const float2 *X0, float2 *cot, const float4 *coef, int nn, int K, int s,
-                              const InstDesc *d, int solves, cudaStream_t st);
 // Fused step boundaries: forward RK4 of step sp (second call; input saved to save_w), state
 // saved to save_x, RK4 of step sn (first call); reverse RK4^T of step sa at Xa then of step
 // sb at Wb. A negative step index skips that half.
