@@ -28,3 +28,11 @@ def test_round_trip_and_tensor(tmp_path):
     save_tensor_real(str(tmp_path), "Tfinal", T)
     line = open(tmp_path / "Tfinal_2.dat").readline()
     assert line == "".join(format(float(x), "g") + "\t" for x in T[2, 0]) + "\n"
+
+
+def test_sweep_folder_names_follow_shg_sh():
+    """SHG.sh:76 names each point's folder from the raw argument text:
+    sPPLT_P_${ARG1}_W_T1_${ARG3}_WAIST_${ARG2}."""
+    from shg_focused_gaussian_beams_gb300.sweep import _folder
+    assert _folder("30", "55.66", "29") == "sPPLT_P_30_W_T1_55.66_WAIST_29"
+    assert _folder("2.5", "50", "31.25") == "sPPLT_P_2.5_W_T1_50_WAIST_31.25"
