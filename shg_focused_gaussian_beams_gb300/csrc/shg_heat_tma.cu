@@ -39,7 +39,7 @@ struct TmaTile {
     // ring of T and Q/k slots, full and empty barriers, slack to align the base to 128 bytes
     static constexpr int SMEM = SLOTS * (T_STRIDE + Q_STRIDE) + 2 * SLOTS * 8 + 128;
 };
-constexpr long long WAIT_LIMIT = 1ll << 22;     // polls before a wait gives up
+constexpr long long WAIT_LIMIT = 1ll << 18;  // polls before a wait gives up (~3.8 us each: ~1 s)
 
 __device__ int g_heat_tma_error;  // 1 once a pipeline wait gave up
 
@@ -82,7 +82,7 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, i
 template <int BC, int RW>
 __global__ void __launch_bounds__(THREADS) k_heat_tma(float *__restrict__ Tf, const __grid_constant__ CUtensorMap mT,
                                                      const __grid_constant__ CUtensorMap mQ, const HeatCoef c, int nx,
-                                                     int ny, int nz, int zc) {
+                                                     int ny, int nz, int zc, int starve) {
     using G = TmaTile<RW>;
     extern __shared__ unsigned char smem_raw[];
     unsigned char *base = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
@@ -104,8 +104,9 @@ __global__ void __launch_bounds__(THREADS) k_heat_tma(float *__restrict__ Tf, co
     }
     __syncthreads();
     if (warp == CONSUMER_WARPS) {
-        // producer: one thread issues the box copies of every plane of the chunk
-        if (lane == 0) {
+        // producer: one thread issues the box copies of every plane of the chunk (none when
+        // `starve` is set: the failure-detection test of the bounded waits)
+        if (lane == 0 && !starve) {
             for (int i = 0; i < np; ++i) {
                 const int s = i % SLOTS;
                 if (i >= SLOTS && !mbar_wait(&empty[s], ((i / SLOTS) - 1) & 1)) break;
@@ -236,7 +237,11 @@ cudaError_t launch_heat_tma_t(float *Tf, const float *Ti, const float *QK, const
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM);
         if (e != cudaSuccess) return e;
     }
-    k<<<grid, THREADS, G::SMEM, st>>>(Tf, mT, mQ, c, nx, ny, nz, zc);
+    // SHG_HEAT_TMA_STARVE=1: the producer issues no copies, so every consumer wait runs out
+    // and sets the error flag (tests the bounded waits and the host's check; no sweep result)
+    const char *sv = std::getenv("SHG_HEAT_TMA_STARVE");
+    const int starve = sv && std::atoi(sv) == 1 ? 1 : 0;
+    k<<<grid, THREADS, G::SMEM, st>>>(Tf, mT, mQ, c, nx, ny, nz, zc, starve);
     return cudaGetLastError();
 }
 

@@ -419,6 +419,7 @@ int shg_heat_sweeps(const shg_config *cfg, float *T_inout, const float *Q, float
     TH_CUDA(cudaMemcpy(ts.T_cur(), T_inout, n * sizeof(float), cudaMemcpyHostToDevice));
     TH_CUDA(cudaMemcpy(ts.T_prev(), T_inout, n * sizeof(float), cudaMemcpyHostToDevice));
     TH_TRY(ts.sweeps(t_inf, nsweeps));
+    TH_TRY(heat_pipeline_ok(ts.stream()));
     return ts.copy_temperature(T_inout);
 }
 

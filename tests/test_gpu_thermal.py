@@ -27,6 +27,29 @@ def _geom(g):
     return dict(lx=float(g["cfg_lx"]), ly=float(g["cfg_ly"]))
 
 
+def test_tma_wait_timeout_is_reported_and_recoverable(monkeypatch):
+    """Failure detection without a GPU fault: with the producer issuing no copies
+    (SHG_HEAT_TMA_STARVE=1) every consumer wait of the TMA-staged sweep runs out after its
+    bounded number of polls, the kernel sets its error flag and returns, and the host call
+    reports the error. The next sweeps in the same process are bit-exact again."""
+    from shg_focused_gaussian_beams_gb300._lib import ShgError
+    monkeypatch.setenv("SHG_HEAT", "tma")
+    monkeypatch.setenv("SHG_HEAT_TB", "1")
+    n, nz = 40, 33
+    o = O.Oracle(O.make_cfg(W.CRYSTAL_QPM50, n, n, nz, 600.0, 600.0))
+    rng = np.random.default_rng(3)
+    T = o.init_temperature(48.0, 50.0, 46.5, 1)
+    T = (T + rng.normal(0, 0.05, T.shape)).astype(np.float32)
+    Q = (rng.random(T.shape) * 5e-9).astype(np.float32)
+    monkeypatch.setenv("SHG_HEAT_TMA_STARVE", "1")
+    with pytest.raises(ShgError, match="TMA pipeline wait gave up"):
+        S.heat_sweeps(W.CRYSTAL_QPM50, T, Q, 25.0, 1, 1, lx=600.0, ly=600.0)
+    monkeypatch.delenv("SHG_HEAT_TMA_STARVE")
+    ref = o.heat_sweeps(T, Q, 25.0, 3, 1)
+    got = S.heat_sweeps(W.CRYSTAL_QPM50, T, Q, 25.0, 3, 1, lx=600.0, ly=600.0)
+    assert bits_equal(got, ref)
+
+
 @pytest.mark.parametrize("name", ["thermal_topopen.npz", "thermal_oven.npz"])
 def test_heat_components_bitexact(name):
     g = golden(name)
