@@ -299,24 +299,73 @@ def run_thermal(args):
     print(json.dumps(line), flush=True)
 
 
-def cpu_sample(insts, cores):
-    """Bounded CPU sample: one solve per core from the workload, N <= 128 and Nz <= 200
-    (the CPU's per-point cost grows with N, so this flatters the CPU)."""
-    pick = [i for i in insts if i.nx <= 128 and i.nz <= 200][:max(1, cores)]
-    return pick or insts[:1]
+CPU_KIND = ("oracle restatement of the reference's z-march (FP32, the reference's operation order) with the "
+            "radix-2 FFTW stand-in of oracle/dft_ref.h, not FFTW (no libfftw3f on the host)")
 
 
-def oracle_rate(sample, cores, reps=1):
+def sweep_classes(insts):
+    """Stratification of a sweep by (N, Nz) class: {(n, nz): (count, first solve of the class)}."""
+    out = {}
+    for i in insts:
+        c, first = out.get((i.nx, i.nz), (0, i))
+        out[(i.nx, i.nz)] = (c + 1, first)
+    return dict(sorted(out.items()))
+
+
+def class_times(classes, copies):
+    """Wall time of `copies` full-length solves of each class run at once on `copies` host
+    threads (the SHG.sh one-process-per-point loop on that many cores): {(n, nz): seconds}."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     cfg = O.make_cfg(W.CRYSTAL_QPM50, 64, 64, 100)
-    O.sweep_plain(cfg, sample[:1], threads=1)  # load / warm
-    times = []
-    for _ in range(reps):
+    out = {}
+    for key, (_, inst) in classes.items():
         t0 = time.perf_counter()
-        O.sweep_plain(cfg, sample, threads=cores)
-        times.append(time.perf_counter() - t0)
-    return pt_steps(sample) / statistics.median(times), times
+        O.sweep_plain(cfg, [inst] * copies, threads=copies)
+        out[key] = time.perf_counter() - t0
+    return out
+
+
+def stratified_rate(classes, per_class_s, cores):
+    """Sweep rate on `cores` host cores from the class times: the 512 solves spread over the
+    cores, so the sweep takes sum over classes of count x (time of one solve) / cores, with one
+    solve's time taken as the wall time of `cores` concurrent solves of its class."""
+    work = sum(c * i.nx * i.ny * i.nz for c, i in classes.values())
+    sweep_s = sum(classes[k][0] * per_class_s[k] for k in classes) / cores
+    return work / sweep_s, sweep_s, work
+
+
+def oracle_rate(insts, cores):
+    """cpu_baseline of the sweep: one full-length solve of each of the (N, Nz) classes, all
+    classes at once on the host cores (bounded: the wall time is the 256x256x400 solve)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    classes = sweep_classes(insts)
+    cfg = O.make_cfg(W.CRYSTAL_QPM50, 64, 64, 100)
+    O.sweep_plain(cfg, [next(iter(classes.values()))[1]], threads=1)  # load / warm
+    reps = [i for _, i in classes.values()]
+    # each class's solve on its own thread, all at once; per-solve time from a timed pass of
+    # each class alone would take longer, so each thread times its own solve
+    import threading as th
+    per = {}
+
+    def one(key, inst):
+        t0 = time.perf_counter()
+        O.sweep_plain(cfg, [inst], threads=1)
+        per[key] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ts = [th.Thread(target=one, args=(k, i)) for k, (_, i) in classes.items()]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    wall = time.perf_counter() - t0
+    value, sweep_s, _ = stratified_rate(classes, per, cores)
+    sample = (f"one full-length solve of each of the {len(reps)} (N, Nz) classes of the sweep, all at once on "
+              f"{len(reps)} of {cores} host threads ({wall:.1f} s wall); sweep time = sum over classes of count x "
+              f"solve time / {cores} cores = {sweep_s:.1f} s; weights (N, Nz: count) "
+              + ", ".join(f"{k[0]}x{k[1]}: {c}" for k, (c, _) in classes.items()))
+    return value, sample
 
 
 class Clocks:
@@ -420,33 +469,57 @@ def allmax(world, v):
 
 
 def run_reference(args):
+    """The reference's CPU algorithm on the sweep, stratified by (N, Nz) class: step k runs
+    full-length solves of the classes assigned to it (every class at least once over the K
+    steps), `cores` copies at once on `cores` host threads, the SHG.sh process-per-point loop.
+    value = the sweep rate derived from the per-class times (stratified_rate)."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     insts, desc = workload(args.workload)
     cores = os.cpu_count() or 1
-    sample = cpu_sample(insts, cores) if args.workload == "sweep" else insts
+    classes = sweep_classes(insts)
+    keys = list(classes)
+    steps = max(args.steps, 1)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     cfg = O.make_cfg(W.CRYSTAL_QPM50, 64, 64, 100)
+    smallest = min(keys, key=lambda k: k[0] * k[0] * k[1])
     for _ in range(args.warmup):
-        O.sweep_plain(cfg, sample[:1], threads=1)
-    times = []
-    for _ in range(args.steps):
+        O.sweep_plain(cfg, [classes[smallest][1]] * cores, threads=cores)
+    per = {k: [] for k in keys}
+    wall = []
+    for k in range(steps):
+        # classes of step k: round robin, so K >= 9 steps cover each class at least once and
+        # fewer steps take several classes each
+        if steps >= len(keys):
+            mine = [keys[k % len(keys)]]
+        else:
+            mine = [keys[j] for j in range(len(keys)) if j % steps == k]
         t0 = time.perf_counter()
-        O.sweep_plain(cfg, sample, threads=cores)
-        times.append(time.perf_counter() - t0)
-    total = sum(times)
-    value = pt_steps(sample) * args.steps / total
+        for key, t in class_times({q: classes[q] for q in mine}, cores).items():
+            per[key].append(t)
+        wall.append(time.perf_counter() - t0)
+    per_s = {k: statistics.median(v) for k, v in per.items() if v}
+    missing = [k for k in keys if k not in per_s]
+    if missing:  # cannot happen with the assignment above; measured here rather than guessed
+        per_s.update(class_times({q: classes[q] for q in missing}, cores))
+    value, sweep_s, work = stratified_rate(classes, per_s, cores)
+    total = sum(wall)
+    sample = (f"each step: full-length solves of its (N, Nz) classes, {cores} copies at once on {cores} host "
+              f"threads; all {len(keys)} classes over the {steps} steps; sweep time on {cores} cores = sum over "
+              f"classes of count x solve time / {cores} = {sweep_s:.1f} s for {len(insts)} solves; weights "
+              "(N x Nz: count) " + ", ".join(f"{k[0]}x{k[1]}: {classes[k][0]}" for k in keys))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": desc | {"sample_solves": len(sample)},
-            "solves_per_s": len(sample) * args.steps / total,
+            "config": desc | {"stratified": {f"{k[0]}x{k[1]}": {"count": classes[k][0],
+                                                                 "solve_s": per_s[k]} for k in keys},
+                              "sweep_s_on_host": sweep_s, "same_config": True},
+            "solves_per_s": len(insts) / sweep_s,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{len(sample)} solves of the workload (N<=128, Nz<=200) per step on "
-                                       f"{cores} threads; oracle restatement of the reference, FP32"},
+                             "sample": sample + "; " + CPU_KIND},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -507,10 +580,12 @@ def run_ours(args):
     solves_s = len(insts) * world * args.steps / (ms * 1e-3)
     eta = sw.results()
 
-    # end to end through the C ABI: parameters in (pinned), efficiencies + SH fields out (pinned)
+    # end to end through the C ABI: parameters in (pinned), efficiencies + the SH and pump
+    # output fields of every solve out (pinned)
     off = sw.field_offsets()
     eta_h = torch.empty(len(insts), dtype=torch.float64, pin_memory=True)
     fld_h = torch.empty(int(off[-1]) * 2, dtype=torch.float32, pin_memory=True)
+    pmp_h = torch.empty(int(off[-1]) * 2, dtype=torch.float32, pin_memory=True)
     eta_np = eta_h.numpy()
     barrier(world)
     torch.cuda.synchronize()
@@ -518,12 +593,14 @@ def run_ours(args):
     for _ in range(args.steps):
         sw.set_instances(insts)
         sw.run(eta_out=eta_np, sh_out_all=fld_h.data_ptr())
+        sw.pump_fields_into(pmp_h.data_ptr())
     torch.cuda.synchronize()
     e2e_s = allmax(world, time.perf_counter() - t0)
     h2d, d2h_fields = sw.io_bytes()
     e2e = {"value": work * world * args.steps / e2e_s, "unit": UNIT,
-           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": len(insts) * 8 + d2h_fields,
-           "solves_per_s": len(insts) * world * args.steps / e2e_s}
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": len(insts) * 8 + 2 * d2h_fields,
+           "solves_per_s": len(insts) * world * args.steps / e2e_s,
+           "outputs": "efficiencies, SH and pump output fields of every solve"}
 
     # the plain per-instance GPU path on a sample of the same solves: one solve at a time
     # through Solver::run (handles created and warmed outside the timed region)
@@ -582,8 +659,7 @@ def run_ours(args):
 
     if rank == 0:
         cores = os.cpu_count() or 1
-        sample = cpu_sample(insts, cores) if args.workload == "sweep" else insts
-        cpu_value, cpu_times = oracle_rate(sample, cores, reps=2)
+        cpu_value, cpu_sample_text = oracle_rate(insts, cores)
         metric = METRIC if args.workload == "sweep" else f"grid-pt·z-steps/s ({desc['workload']})"
         line = {"metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -594,8 +670,7 @@ def run_ours(args):
                 "solves_per_s": solves_s, "e2e": e2e, "gpu_launches": launches * args.steps,
                 "roofline": roof, "clocks": clk.summary(),
                 "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": cores, "kind": "port",
-                                 "sample": f"{len(sample)} solves of the workload (N<=128, Nz<=200) on {cores} "
-                                           f"threads, median of {len(cpu_times)} runs; oracle restatement, FP32"},
+                                 "sample": cpu_sample_text + "; " + CPU_KIND},
                 "eta_mean": float(np.mean(eta)),
                 "per_instance_gpu": per,
                 "batched_over_per_instance": {"solves_per_s": solves_s / world / per["solves_per_s"],

@@ -97,6 +97,18 @@ const char *shg_last_error(void);
  * Synchronises `stream`. */
 int shg_grad_device(shg_handle *h, float temp, const void *pump_in, const void *sh_in, int checkpoints,
                     void *grad_pump, void *grad_sh, double *out4, void *stream);
+/* Gradient of the SH output power of Solver::run's plain path (Solver.h:342-348): the input
+ * pump is the focused Gaussian of setPump (Efields.h:74-104, index at `temp`) of (power,
+ * waist, focalpoint), times pump_factor when given (device, NX*NY complex64, e.g. a seeded
+ * perturbation; NULL: 1); the SH starts at zero; propagators and delta-k at `temp`.
+ * grad_pump (device, may be NULL) receives dL/dA of the input pump A (dL/dRe + i dL/dIm).
+ * out8: [0] L (W), [1] dL/dT with the input field held fixed (W/K), [2] dL/dLambda (W/um),
+ * [3] dL/d(delta k) (W um), [4] dL/dfocalpoint (W/um), [5] dL/dwaist (W/um), [6] dL/dPower
+ * (W/W), [7] dL/dT including the pump's index n_p(T) (W/K). The pump-parameter terms are
+ * FP64 sums of the adjoint field against the analytic derivatives of setPump. Synchronises
+ * `stream`. */
+int shg_grad_run(shg_handle *h, float power, float waist, float focalpoint, float temp, const void *pump_factor,
+                 int checkpoints, void *grad_pump, double *out8, void *stream);
 /* Changes the poling period (Crystal.h:43) of a plain handle for the following runs. */
 int shg_set_poling_period(shg_handle *h, float lambda_qpm);
 
@@ -140,7 +152,11 @@ int shg_batch_create(const shg_config *crystal, const shg_instance *inst, int n,
 int shg_batch_destroy(shg_batch *b);
 /* Runs every solve and copies the efficiencies (n doubles) to the host; when sh_out_all
  * is not NULL it receives the SH output fields of all solves back to back in solve order
- * (solve i at the complex offset given by shg_batch_field_offsets). */
+ * (solve i at the complex offset given by shg_batch_field_offsets). A batch whose device
+ * memory exceeds the free memory returns SHG_ERR_NOMEM from shg_batch_create (checked on
+ * the host before allocating). When a solve's efficiency is NaN or infinite (e.g. a NaN
+ * parameter), every value is still stored and SHG_ERR_NONFINITE names the first such
+ * solve (also from shg_batch_results). */
 int shg_batch_run(shg_batch *b, double *eta, float *sh_out_all);
 /* After a run: output pump and SH fields of all solves (same layout as sh_out_all above);
  * either pointer may be NULL. */
@@ -206,7 +222,9 @@ int shg_batch_profile(shg_batch *b, shg_kernel_stat *stats, int max_stats, int *
  * caller-owned device buffers of NX*NY complex64; when eta is not NULL the call
  * synchronises `stream` and stores the efficiency. The first call on a device, with that
  * device current, does a one-time set-up (array address, twiddle tables); make it before
- * any stream capture. All calls share the array: calls that overlap on the GPU race. */
+ * any stream capture. That set-up is cached per device ordinal for the process, so a
+ * device reset after the first call is not supported. All calls share the array and it
+ * keeps the last call's contents: calls that overlap on the GPU race. */
 int shg_cwes_noalloc(const shg_config *cfg, float temp, const void *pump_in, const void *sh_in,
                      void *pump_out, void *sh_out, double *eta, void *stream);
 

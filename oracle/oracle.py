@@ -60,6 +60,7 @@ def lib():
         L.oracle_run_plain_f32.argtypes = [P, _f, _f, _f, _f, _i, _pf, _pf]
         L.oracle_init_temperature.argtypes = [P, _f, _f, _f, _i, _pf]
         L.oracle_heat_sweeps.argtypes = [P, _pf, _pf, _f, _i, _i]
+        L.oracle_set_threads.argtypes = [_i]
         L.oracle_reduced_sum.restype = _f
         L.oracle_reduced_sum.argtypes = [P, _pf, _pf]
         L.oracle_dk_thermal.argtypes = [P, _pf, _pf]
@@ -73,6 +74,11 @@ def lib():
         L.oracle_power_f32.argtypes = [P, _pf, _f]
         _lib = L
     return _lib
+
+
+def set_threads(threads: int):
+    """Host threads of the restatement's heat sweeps (results do not depend on it)."""
+    lib().oracle_set_threads(int(threads))
 
 
 def _pF(a):

@@ -4,6 +4,7 @@
 // path is the same method in double.
 #include "shg_oracle.h"
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstring>
@@ -431,13 +432,17 @@ struct HeatCoef {
     }
 };
 
-// One sweep of Tfield.h:113-221 (bc 0) or Tfield.h:224-258 (bc 1): Tf from Ti. Voxels
-// that the reference never writes keep Tf's current value.
-void heat_sweep(const Model<float> &m, const HeatCoef &c, float *Tf, const float *Ti, float T_inf,
-                const float *Q, int bc) {
+// Host threads of the heat sweep (oracle_set_threads). Every voxel of a sweep depends only
+// on the previous sweep's field, so splitting the z range over threads changes no result.
+static int g_heat_threads = 1;
+
+// One sweep of Tfield.h:113-221 (bc 0) or Tfield.h:224-258 (bc 1), planes [z0, z1): Tf from
+// Ti. Voxels that the reference never writes keep Tf's current value.
+void heat_sweep_planes(const Model<float> &m, const HeatCoef &c, float *Tf, const float *Ti, float T_inf,
+                       const float *Q, int bc, int z0, int z1) {
     const int NX = m.NX, NY = m.NY, NZ = m.NZ;
     auto I = [&](int x, int y, int z) { return m.idx(x, y, z); };
-    for (int z = 0; z < NZ; ++z)
+    for (int z = z0; z < z1; ++z)
         for (int y = 0; y < NY; ++y)
             for (int x = 0; x < NX; ++x) {
                 const bool xi = x > 0 && x < NX - 1, yi = y > 0 && y < NY - 1, zi = z > 0 && z < NZ - 1;
@@ -486,6 +491,20 @@ void heat_sweep(const Model<float> &m, const HeatCoef &c, float *Tf, const float
                           T_inf * c.BiD) * c.GV;
                 }
             }
+}
+
+void heat_sweep(const Model<float> &m, const HeatCoef &c, float *Tf, const float *Ti, float T_inf,
+                const float *Q, int bc) {
+    const int NZ = m.NZ, nt = std::max(1, std::min(g_heat_threads, NZ));
+    if (nt == 1) {
+        heat_sweep_planes(m, c, Tf, Ti, T_inf, Q, bc, 0, NZ);
+        return;
+    }
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; ++t)
+        pool.emplace_back(heat_sweep_planes, std::cref(m), std::cref(c), Tf, Ti, T_inf, Q, bc, NZ * t / nt,
+                          NZ * (t + 1) / nt);
+    for (auto &th : pool) th.join();
 }
 
 // Tfield.h:13-28
@@ -623,15 +642,19 @@ void oracle_init_temperature(const oracle_cfg *c, float temp, float t1, float t2
     init_temperature(m, T, temp, t1, t2, bc);
 }
 
+void oracle_set_threads(int threads) { g_heat_threads = threads < 1 ? 1 : threads; }
+
+// Tinic <- Tfinal after every sweep (Solver.h:321) is a swap of the two buffers here: the
+// voxels a sweep never writes are equal in both, so the next sweep sees the same input.
 void oracle_heat_sweeps(const oracle_cfg *c, float *T, const float *Q, float t_inf, int nsweeps, int bc) {
     Model<float> m(*c);
     HeatCoef hc(m);
     std::vector<float> Tf(T, T + m.TSIZE), Ti(T, T + m.TSIZE);
     for (int k = 0; k < nsweeps; ++k) {
         heat_sweep(m, hc, Tf.data(), Ti.data(), t_inf, Q, bc);
-        std::memcpy(Ti.data(), Tf.data(), m.TSIZE * sizeof(float));
+        std::swap(Ti, Tf);
     }
-    std::memcpy(T, Tf.data(), m.TSIZE * sizeof(float));
+    std::memcpy(T, Ti.data(), m.TSIZE * sizeof(float));
 }
 
 float oracle_reduced_sum(const oracle_cfg *c, const float *Tf, const float *Ti) {
@@ -681,9 +704,10 @@ int oracle_thermal_run(const oracle_cfg *c, float power, float waist, float foca
                 Reduced_sum = reduced_sum(m, Tf.data(), Ti.data());
                 if (Reduced_sum == aux_sum) Reduced_sum = (float)(0.5 * (D)tol);
             }
-            std::memcpy(Ti.data(), Tf.data(), m.TSIZE * sizeof(float));
+            std::swap(Ti, Tf);  // Tinic <- Tfinal (Solver.h:321): both now hold the new field
             counter_T++;
         }
+        Tf = Ti;
         counts[outer++] = (int)counter_T;
         dk_thermal<float>(m, Tf.data(), DK.data());
         const float tc = Tf[m.idx(m.NX / 2, m.NY / 2, 0)];

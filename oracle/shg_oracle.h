@@ -70,6 +70,8 @@ void oracle_run_plain_f32(const oracle_cfg *c, float power, float waist, float f
  * bc 1 = oven surrounded (Tfield.h:224). */
 void oracle_init_temperature(const oracle_cfg *c, float temp, float t1, float t2, int bc, float *T);
 void oracle_heat_sweeps(const oracle_cfg *c, float *T, const float *Q, float t_inf, int nsweeps, int bc);
+/* Host threads of the heat sweeps (default 1); the results do not depend on it. */
+void oracle_set_threads(int threads);
 float oracle_reduced_sum(const oracle_cfg *c, const float *Tf, const float *Ti);
 void oracle_dk_thermal(const oracle_cfg *c, const float *T, float *DK);
 void oracle_set_q(const oracle_cfg *c, const float *T, const float *pump, const float *sh, int s, float *Q);

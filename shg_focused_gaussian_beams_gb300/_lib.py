@@ -73,6 +73,7 @@ SIGNATURES = {
     "shg_batch_io_bytes": (_i, [_vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "shg_dft2d_device": (_i, [_i, _i, _vp, _vp, _vp]),
     "shg_grad_device": (_i, [_vp, _f, _vp, _vp, _i, _vp, _vp, _pd, _vp]),
+    "shg_grad_run": (_i, [_vp, _f, _f, _f, _f, _vp, _i, _vp, _pd, _vp]),
     "shg_set_poling_period": (_i, [_vp, _f]),
     "shg_set_output_dir": (_i, [_vp, C.c_char_p]),
     "shg_get_temperature": (_i, [_vp, _pf]),

@@ -7,6 +7,12 @@ adjoint (``shg_grad_device``), with the checkpoint count of the solver wrapper. 
 pump with torch operations (e.g. ``gaussian_pump``) to carry gradients on to its own
 parameters (focus position, waist, power).
 
+``run_power(solver, power, waist, focal, temp, lambda_qpm)`` is Solver::run's plain path
+(Gaussian pump of setPump, optionally times a fixed complex factor) and back-propagates to
+the focal point, waist, pump power, oven temperature (through the pump's index as well) and
+poling period with the gradients the C ABI returns (``shg_grad_run``): the pump-parameter
+derivatives are formed on the device, with no torch restatement of the pump.
+
 ``thermal_batch_power(batch, pumps)`` does the same for a batch of THERMAL solves whose
 temperature fields are held fixed (``shg_thgrad_gradient``), differentiable in the pumps.
 """
@@ -49,6 +55,30 @@ def shg_power(solver, pump, temp, lambda_qpm, checkpoints=20):
     temp = torch.as_tensor(temp, dtype=torch.float64, device=pump.device)
     lam = torch.as_tensor(lambda_qpm, dtype=torch.float64, device=pump.device)
     return _SHGPower.apply(pump, temp, lam, solver, checkpoints)
+
+
+class _RunPower(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, power, waist, focal, temp, lam, solver, factor, checkpoints):
+        if float(lam) != solver.cfg.lambda_qpm:
+            solver.set_poling_period(float(lam))
+        r = solver.grad_run(float(power), float(waist), float(focal), float(temp), pump_factor=factor,
+                            checkpoints=checkpoints, device=power.device)
+        ctx.grads = (r["dpower"], r["dwaist"], r["dfocal"], r["dT_total"], r["dLambda"])
+        return torch.tensor(r["loss"], dtype=torch.float64, device=power.device)
+
+    @staticmethod
+    def backward(ctx, g):
+        gs = [(g * d).reshape(()).to(torch.float64) for d in ctx.grads]
+        return gs[0], gs[1], gs[2], gs[3], gs[4], None, None, None
+
+
+def run_power(solver, power, waist, focal, temp, lambda_qpm, pump_factor=None, checkpoints=20, device="cuda"):
+    """SH output power (W) of Solver::run's plain path, differentiable in the pump power,
+    waist, focal point, oven temperature and poling period (pump_factor is held fixed)."""
+    args = [torch.as_tensor(v, dtype=torch.float64, device=device)
+            for v in (power, waist, focal, temp, lambda_qpm)]
+    return _RunPower.apply(*args, solver, pump_factor, checkpoints)
 
 
 class _ThermalBatchPower(torch.autograd.Function):

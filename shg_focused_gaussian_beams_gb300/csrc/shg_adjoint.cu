@@ -280,6 +280,74 @@ __global__ void k_seed_cotangent(const float2 *__restrict__ S, float2 *cP, float
     }
 }
 
+// Parameter sensitivities of the focused Gaussian pump of Efields.h:74-104 (setPump),
+//   G = (Ap0 / M) exp(X),  X = -r^2 / (w^2 M),  M = 1 - i f / zR,
+//   Ap0 = sqrt(4 P / (eps0 c pi n w^2)),  zR = pi n w^2 / lp,
+// evaluated in FP64 per grid point: with the input A = G * factor and the cotangent g of A
+// (dL/dRe + i dL/dIm), out[k] += sum Re(conj(g) dA/dtheta_k) for theta = (f, w, P, n):
+//   dG/dM = G (-1/M + r^2/(w^2 M^2)),  dM/df = -i/zR,  dM/dw = 2 i f/(zR w),  dM/dn = i f/(zR n),
+//   dG/dw = G (-1/w + 2 r^2/(w^3 M)) + dG/dM dM/dw,  dG/dP = G/(2P),  dG/dn = -G/(2n) + dG/dM dM/dn.
+// r^2 uses the reference's centre (0.5 NX, 0.5 NY) and float coordinates ((i - u) dx).
+struct PumpParams {
+    int n;
+    float uX, uY, dx, dy;
+    double ap0, zr, w, f, power, nidx;
+};
+
+__device__ __forceinline__ double2 z_mul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 z_div(double2 a, double2 b) {
+    const double d = b.x * b.x + b.y * b.y;
+    return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
+
+__global__ void k_pump_param_sums(const float2 *__restrict__ g, const float2 *__restrict__ factor, PumpParams p,
+                                  double *out) {
+    double a[4] = {0.0, 0.0, 0.0, 0.0};
+    const int nn = p.n * p.n;
+    const double2 M = make_double2(1.0, -p.f / p.zr);
+    const double2 one = make_double2(1.0, 0.0);
+    const double2 invM = z_div(one, M), invM2 = z_mul(invM, invM);
+    const double w2 = p.w * p.w;
+    const double2 dMf = make_double2(0.0, -1.0 / p.zr);
+    const double2 dMw = make_double2(0.0, 2.0 * p.f / (p.zr * p.w));
+    const double2 dMn = make_double2(0.0, p.f / (p.zr * p.nidx));
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += gridDim.x * blockDim.x) {
+        const int ix = i % p.n, iy = i / p.n;
+        const double x = (double)((float)ix - p.uX) * (double)p.dx, y = (double)((float)iy - p.uY) * (double)p.dy;
+        const double r2 = x * x + y * y;
+        // G = Ap0/M exp(-r^2/(w^2 M))
+        const double2 X = make_double2(-r2 / w2 * invM.x, -r2 / w2 * invM.y);
+        const double ex = exp(X.x);
+        double sn, cs;
+        sincos(X.y, &sn, &cs);
+        const double2 G = z_mul(make_double2(p.ap0 * invM.x, p.ap0 * invM.y), make_double2(ex * cs, ex * sn));
+        // dG/dM = G (-1/M + r^2/(w^2 M^2))
+        const double2 q = make_double2(-invM.x + r2 / w2 * invM2.x, -invM.y + r2 / w2 * invM2.y);
+        const double2 dGdM = z_mul(G, q);
+        const double2 dGf = z_mul(dGdM, dMf);
+        const double2 tw = make_double2(-1.0 / p.w + 2.0 * r2 / (w2 * p.w) * invM.x, 2.0 * r2 / (w2 * p.w) * invM.y);
+        const double2 dGw0 = z_mul(G, tw), dGw1 = z_mul(dGdM, dMw);
+        const double2 dGw = make_double2(dGw0.x + dGw1.x, dGw0.y + dGw1.y);
+        const double2 dGP = make_double2(G.x / (2.0 * p.power), G.y / (2.0 * p.power));
+        const double2 dGn1 = z_mul(dGdM, dMn);
+        const double2 dGn = make_double2(-G.x / (2.0 * p.nidx) + dGn1.x, -G.y / (2.0 * p.nidx) + dGn1.y);
+        const float2 fc = factor ? factor[i] : make_float2(1.f, 0.f);
+        const double2 fd = make_double2(fc.x, fc.y);
+        const float2 gv = g[i];
+        const double2 ds[4] = {z_mul(dGf, fd), z_mul(dGw, fd), z_mul(dGP, fd), z_mul(dGn, fd)};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) a[k] += (double)gv.x * ds[k].x + (double)gv.y * ds[k].y;
+    }
+    block_sum_doubles(a, 4, out);
+}
+
+// A *= factor (complex), elementwise.
+__global__ void k_cmul_inplace(float2 *A, const float2 *__restrict__ factor, int nn) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += gridDim.x * blockDim.x) A[i] = c_mul(A[i], factor[i]);
+}
+
 static int grid_for(int nn) {
     int b = (nn + 255) / 256;
     return b < 1216 ? b : 1216;
@@ -372,6 +440,21 @@ cudaError_t launch_abs2_sum(const float2 *S, int nn, double *out, cudaStream_t s
 
 cudaError_t launch_seed_cotangent(const float2 *S, float2 *cP, float2 *cS, int nn, const double *g, cudaStream_t st) {
     k_seed_cotangent<<<grid_for(nn), 256, 0, st>>>(S, cP, cS, nn, g);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pump_param_sums(const float2 *g, const float2 *factor, int n, float uX, float uY, float dx, float dy,
+                                   double ap0, double zr, double w, double f, double power, double nidx, double *out,
+                                   cudaStream_t st) {
+    const PumpParams p{n, uX, uY, dx, dy, ap0, zr, w, f, power, nidx};
+    cudaError_t e = cudaMemsetAsync(out, 0, 4 * sizeof(double), st);
+    if (e != cudaSuccess) return e;
+    k_pump_param_sums<<<grid_for(n * n), 256, 0, st>>>(g, factor, p, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cmul_inplace(float2 *A, const float2 *factor, int nn, cudaStream_t st) {
+    k_cmul_inplace<<<grid_for(nn), 256, 0, st>>>(A, factor, nn);
     return cudaGetLastError();
 }
 

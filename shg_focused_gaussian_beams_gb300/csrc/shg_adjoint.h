@@ -26,6 +26,12 @@ cudaError_t launch_adj_rows_bwd(int n, const InstDesc *d, float2 *C, int s, int 
                                 const float2 *Wn, double *acc_fin, double *acc_start, cudaStream_t st);
 cudaError_t launch_abs2_sum(const float2 *S, int nn, double *out, cudaStream_t st);
 cudaError_t launch_seed_cotangent(const float2 *S, float2 *cP, float2 *cS, int nn, const double *g, cudaStream_t st);
+// out[0..4) = sum Re(conj(g) dA/dtheta) for theta = focal point, waist, power, pump index,
+// where A = (Gaussian pump of Efields.h:74-104) * factor (factor NULL: 1); FP64.
+cudaError_t launch_pump_param_sums(const float2 *g, const float2 *factor, int n, float uX, float uY, float dx, float dy,
+                                   double ap0, double zr, double w, double f, double power, double nidx, double *out,
+                                   cudaStream_t st);
+cudaError_t launch_cmul_inplace(float2 *A, const float2 *factor, int nn, cudaStream_t st);
 
 // Device work space of one gradient pass.
 struct AdjointWork {
@@ -49,5 +55,11 @@ struct AdjointWork {
 // (SH output power, W), out[1] = dL/dT, out[2] = dL/dLambda, out[3] = dL/d(delta k).
 int adjoint_run(const shg_config &cfg, const InstDesc &h, const InstDesc *d, float temp, int checkpoints,
                 AdjointWork &w, cudaStream_t st, float2 *grad_pump, float2 *grad_sh, double *out);
+// After adjoint_run for an input pump A = (Gaussian of (power, waist, focal) at index
+// temperature temp) * factor: out4 = dL/dfocal, dL/dwaist, dL/dpower, dL/dT through the
+// pump's index n_p(T) (setPump evaluates n at the run temperature).
+int pump_param_gradients(const shg_config &cfg, const InstDesc &h, float power, float waist, float focal, float temp,
+                         const float2 *factor, AdjointWork &w, cudaStream_t st, double *out4);
+double sellmeier_dT(double L, double T);
 
 }  // namespace shg

@@ -63,6 +63,10 @@ int AdjointWork::ensure(int n_, int K_, int L_, int nck_) {
     const size_t st = 2 * nn;
     const size_t sets = nck > 0 ? 2 : 1;
     bytes = sizeof(float2) * (st * (2 + (size_t)nck + 3 * sets * (size_t)L)) + sizeof(double) * (8 * (size_t)K + 8);
+    {
+        const int rc = device_fits(bytes, "gradient work space");
+        if (rc) return rc;
+    }
     AD_CUDA(cudaMalloc(&mem, bytes));
     float2 *p = reinterpret_cast<float2 *>(mem);
     X = p;
@@ -83,7 +87,7 @@ int AdjointWork::ensure(int n_, int K_, int L_, int nck_) {
 }
 
 // dn/dT of Crystal.h:116-132 in double (the smooth model behind the float index).
-static double sellmeier_dT(double L, double T) {
+double sellmeier_dT(double L, double T) {
     const double A = 4.502483, B = 0.007294, C = 0.185087, D = -0.02357, E = 0.073423, F = 0.199595, G = 0.001,
                  H = 7.99724;
     const double tk = T + 273.15;
@@ -252,6 +256,28 @@ int adjoint_run(const shg_config &cfg, const InstDesc &h, const InstDesc *d, flo
     out[1] = dT;
     out[2] = dL_ddk * (-two_pi / (lam * lam));
     out[3] = dL_ddk;
+    return SHG_OK;
+}
+
+int pump_param_gradients(const shg_config &cfg, const InstDesc &h, float power, float waist, float focal, float temp,
+                         const float2 *factor, AdjointWork &w, cudaStream_t st, double *out4) {
+    // Efields.h:74-104 constants in double from the float index the reference uses
+    const double PI = 3.14159265358979323846;
+    const double eps0 = (double)(float)(8.8541878128E-12 * 1E12 / 1E6), c = (double)(float)(299792458 * 1E6 / 1E12);
+    const double np = (double)sellmeier(cfg.lp, temp);
+    const double w_ = waist, w2 = w_ * w_;
+    const double zr = PI * np * w2 / (double)cfg.lp;
+    const double ap0 = std::sqrt(4.0 * (double)power / (eps0 * c * PI * np * w2));
+    double *sums = w.acc_glob + 4;  // [4..7] free in the global sums
+    AD_CUDA(launch_pump_param_sums(w.cot, factor, h.n, h.uX, h.uY, h.dx, h.dy, ap0, zr, w_, (double)focal,
+                                   (double)power, np, sums, st));
+    double r[4];
+    AD_CUDA(cudaMemcpyAsync(r, sums, sizeof(r), cudaMemcpyDeviceToHost, st));
+    AD_CUDA(cudaStreamSynchronize(st));
+    out4[0] = r[0];
+    out4[1] = r[1];
+    out4[2] = r[2];
+    out4[3] = r[3] * sellmeier_dT(cfg.lp, temp);
     return SHG_OK;
 }
 

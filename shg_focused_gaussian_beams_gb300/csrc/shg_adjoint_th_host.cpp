@@ -71,6 +71,8 @@ int ThermalGradBatch::create(const shg_config &cfg, int count) {
     TG_CUDA(cudaSetDevice(cfg.device));
     TG_TRY(ensure_twiddles(cfg.device));
     const size_t c = (size_t)count;
+    TG_TRY(device_fits(c * (tsize_ * sizeof(float) + (size_t)K_ * nn_ * sizeof(float4) + 3 * nn_ * sizeof(float2)),
+                       "batched THERMAL gradient"));
     TG_CUDA(cudaMalloc(&T_, c * tsize_ * sizeof(float)));
     TG_CUDA(cudaMalloc(&coef_, c * (size_t)K_ * nn_ * sizeof(float4)));
     TG_CUDA(cudaMalloc(&props_, c * 2 * nn_ * sizeof(float2)));
@@ -177,6 +179,7 @@ int ThermalGradBatch::ensure_work(int L, int nck) {
     const size_t st = (size_t)count_ * 2 * nn_;
     work_bytes_ = sizeof(float2) * ((size_t)count_ * nn_ + st * (2 + (size_t)nck + 2 * (size_t)L)) +
                   sizeof(double) * 2 * (size_t)count_;
+    TG_TRY(device_fits(work_bytes_, "batched THERMAL gradient work space"));
     TG_CUDA(cudaMalloc(&work_, work_bytes_));
     float2 *p = static_cast<float2 *>(work_);
     in_ = p;

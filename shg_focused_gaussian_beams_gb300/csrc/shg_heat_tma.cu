@@ -7,7 +7,8 @@
 // and the 32 x 8 RW Q/k box of the tile. Eight consumer warps compute RW voxels each per
 // plane from the ring (x/y neighbours from plane z, z neighbours from planes z -+ 1) and
 // store them. Full and empty mbarriers order the ring; every wait is bounded and a timeout
-// sets an error flag that the host reads, instead of hanging.
+// sets the caller's error word (one per solve or call, passed to the kernel) that the host
+// reads, instead of hanging.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -17,6 +18,7 @@
 #include <map>
 #include <mutex>
 #include <tuple>
+#include <vector>
 
 #include "shg_internal.h"
 #include "shg_thermal.cuh"
@@ -41,8 +43,6 @@ struct TmaTile {
 };
 constexpr long long WAIT_LIMIT = 1ll << 18;  // polls before a wait gives up (~3.8 us each: ~1 s)
 
-__device__ int g_heat_tma_error;  // 1 once a pipeline wait gave up
-
 __device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 
 __device__ __forceinline__ void mbar_init(uint64_t *b, unsigned count) {
@@ -64,11 +64,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *b, unsigned parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait: false (and the error flag set) if the phase did not complete.
-__device__ __forceinline__ bool mbar_wait(uint64_t *b, unsigned parity) {
+// Bounded wait: false (and *err set to 1) if the phase did not complete.
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, unsigned parity, int *err) {
     for (long long it = 0; it < WAIT_LIMIT; ++it)
         if (mbar_try_wait(b, parity)) return true;
-    atomicExch(&g_heat_tma_error, 1);
+    atomicExch(err, 1);
     return false;
 }
 __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z, uint64_t *bar) {
@@ -82,7 +82,7 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, i
 template <int BC, int RW>
 __global__ void __launch_bounds__(THREADS) k_heat_tma(float *__restrict__ Tf, const __grid_constant__ CUtensorMap mT,
                                                      const __grid_constant__ CUtensorMap mQ, const HeatCoef c, int nx,
-                                                     int ny, int nz, int zc, int starve) {
+                                                     int ny, int nz, int zc, int starve, int *err) {
     using G = TmaTile<RW>;
     extern __shared__ unsigned char smem_raw[];
     unsigned char *base = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
@@ -107,16 +107,20 @@ __global__ void __launch_bounds__(THREADS) k_heat_tma(float *__restrict__ Tf, co
         // producer: one thread issues the box copies of every plane of the chunk (none when
         // `starve` is set: the failure-detection test of the bounded waits)
         if (lane == 0 && !starve) {
+            int issued = 0;
             for (int i = 0; i < np; ++i) {
                 const int s = i % SLOTS;
-                if (i >= SLOTS && !mbar_wait(&empty[s], ((i / SLOTS) - 1) & 1)) break;
+                if (i >= SLOTS && !mbar_wait(&empty[s], ((i / SLOTS) - 1) & 1, err)) break;
                 mbar_expect_tx(&full[s], G::T_BYTES + G::Q_BYTES);
                 const int p = z0 - 1 + i;
                 tma_load_3d(sT + s * TS, &mT, x0 - XOFF, y0 - 1, p, &full[s]);
                 tma_load_3d(sQ + s * QS, &mQ, x0, y0, p, &full[s]);
+                issued = i + 1;
             }
-            // copies still in flight complete before the block may exit
-            for (int i = np - SLOTS < 0 ? 0 : np - SLOTS; i < np; ++i) mbar_wait(&full[i % SLOTS], (i / SLOTS) & 1);
+            // copies still in flight complete before the block may exit; only planes that
+            // were issued are waited for (after an early break the rest never arrive)
+            for (int i = issued - SLOTS < 0 ? 0 : issued - SLOTS; i < issued; ++i)
+                mbar_wait(&full[i % SLOTS], (i / SLOTS) & 1, err);
         }
         return;
     }
@@ -132,11 +136,11 @@ __global__ void __launch_bounds__(THREADS) k_heat_tma(float *__restrict__ Tf, co
         colint[r] = x > 0 && x < nx - 1 && y > 0 && y < ny - 1;
         ci[r] = (ty + 1) * BX + lane + XOFF;  // this voxel in a T box
     }
-    if (!mbar_wait(&full[0], 0) || !mbar_wait(&full[1], 0)) return;
+    if (!mbar_wait(&full[0], 0, err) || !mbar_wait(&full[1], 0, err)) return;
     for (int z = z0; z < z1; ++z) {
         const int i = z - z0 + 1;  // relative plane index of z
         const int sm = (i - 1) % SLOTS, s0 = i % SLOTS, sp = (i + 1) % SLOTS;
-        if (!mbar_wait(&full[sp], ((i + 1) / SLOTS) & 1)) return;
+        if (!mbar_wait(&full[sp], ((i + 1) / SLOTS) & 1, err)) return;
         const float *P = sT + s0 * TS;
         const bool zint = z > 0 && z < nz - 1;
 #pragma unroll
@@ -223,7 +227,7 @@ int heat_tma_chunk(int nz) {
 
 template <int RW>
 cudaError_t launch_heat_tma_t(float *Tf, const float *Ti, const float *QK, const HeatCoef &c, int nx, int ny,
-                              int nz, int bc, cudaStream_t st) {
+                              int nz, int bc, int *err, cudaStream_t st) {
     using G = TmaTile<RW>;
     CUtensorMap mT, mQ;
     cudaError_t e = tensor_map(Ti, nx, ny, nz, BX, G::BY, &mT);
@@ -241,7 +245,7 @@ cudaError_t launch_heat_tma_t(float *Tf, const float *Ti, const float *QK, const
     // and sets the error flag (tests the bounded waits and the host's check; no sweep result)
     const char *sv = std::getenv("SHG_HEAT_TMA_STARVE");
     const int starve = sv && std::atoi(sv) == 1 ? 1 : 0;
-    k<<<grid, THREADS, G::SMEM, st>>>(Tf, mT, mQ, c, nx, ny, nz, zc, starve);
+    k<<<grid, THREADS, G::SMEM, st>>>(Tf, mT, mQ, c, nx, ny, nz, zc, starve, err);
     return cudaGetLastError();
 }
 
@@ -251,26 +255,64 @@ bool heat_tma_supported(int nx, int ny, int nz) {
 }
 
 cudaError_t launch_heat_tma(float *Tf, const float *Ti, const float *QK, const HeatCoef &c, int nx, int ny, int nz,
-                            int bc, cudaStream_t st, int rows_per_warp) {
-    if (!heat_tma_supported(nx, ny, nz) || (reinterpret_cast<uintptr_t>(Ti) & 15) ||
+                            int bc, int *err, cudaStream_t st, int rows_per_warp) {
+    if (!heat_tma_supported(nx, ny, nz) || !err || (reinterpret_cast<uintptr_t>(Ti) & 15) ||
         (reinterpret_cast<uintptr_t>(QK) & 15))
         return cudaErrorInvalidValue;
     switch (rows_per_warp) {
-        case 1: return launch_heat_tma_t<1>(Tf, Ti, QK, c, nx, ny, nz, bc, st);
-        case 2: return launch_heat_tma_t<2>(Tf, Ti, QK, c, nx, ny, nz, bc, st);
-        case 4: return launch_heat_tma_t<4>(Tf, Ti, QK, c, nx, ny, nz, bc, st);
-        case 8: return launch_heat_tma_t<8>(Tf, Ti, QK, c, nx, ny, nz, bc, st);
+        case 1: return launch_heat_tma_t<1>(Tf, Ti, QK, c, nx, ny, nz, bc, err, st);
+        case 2: return launch_heat_tma_t<2>(Tf, Ti, QK, c, nx, ny, nz, bc, err, st);
+        case 4: return launch_heat_tma_t<4>(Tf, Ti, QK, c, nx, ny, nz, bc, err, st);
+        case 8: return launch_heat_tma_t<8>(Tf, Ti, QK, c, nx, ny, nz, bc, err, st);
         default: return cudaErrorInvalidValue;
     }
 }
 
-// Reads and clears the pipeline error flag (1: a wait gave up, the sweep is incomplete).
-cudaError_t heat_tma_error(int *flag, cudaStream_t st) {
-    int zero = 0;
-    cudaError_t e = cudaMemcpyFromSymbolAsync(flag, g_heat_tma_error, sizeof(int), 0, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(g_heat_tma_error, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, st);
+// Reads and clears the error word `err` on `st` (1: a wait gave up, the sweep is incomplete).
+cudaError_t heat_tma_error(int *err, int *flag, cudaStream_t st) {
+    cudaError_t e = cudaMemcpyAsync(flag, err, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, sizeof(int), st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     return e;
+}
+
+// Error words of component calls that own no solve (shg_heat_sweeps_device): a pool of
+// device ints, each leased to one call at a time and returned cleared.
+namespace {
+std::mutex g_err_mu;
+std::map<int, std::vector<int *>> g_err_free;  // per device ordinal
+}  // namespace
+
+cudaError_t heat_error_word_acquire(int **err) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    {
+        std::lock_guard<std::mutex> lock(g_err_mu);
+        auto &v = g_err_free[dev];
+        if (!v.empty()) {
+            *err = v.back();
+            v.pop_back();
+            return cudaSuccess;
+        }
+    }
+    int *p = nullptr;
+    e = cudaMalloc(&p, sizeof(int));
+    if (e != cudaSuccess) return e;
+    e = cudaMemset(p, 0, sizeof(int));
+    if (e != cudaSuccess) {
+        cudaFree(p);
+        return e;
+    }
+    *err = p;
+    return cudaSuccess;
+}
+
+void heat_error_word_release(int *err) {
+    int dev = 0;
+    if (!err || cudaGetDevice(&dev) != cudaSuccess) return;
+    std::lock_guard<std::mutex> lock(g_err_mu);
+    g_err_free[dev].push_back(err);
 }
 
 }  // namespace shg

@@ -133,6 +133,19 @@ double field_power(double sum_abs2, float n_index, float dx, float dy) {
     return 0.5 * (double)ph.EPS0 * (double)ph.C * (double)n_index * sum_abs2 * (double)dx * (double)dy;
 }
 
+// SHG_ERR_NOMEM, checked on the host, when `bytes` exceed the free memory of the current
+// device: a request that cannot fit is refused before it reaches the allocator.
+int device_fits(size_t bytes, const char *what) {
+    size_t free_b = 0, total_b = 0;
+    SHG_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    if (bytes > free_b) {
+        set_error(std::string(what) + ": needs " + std::to_string(bytes >> 20) + " MiB of device memory, " +
+                  std::to_string(free_b >> 20) + " MiB free");
+        return SHG_ERR_NOMEM;
+    }
+    return SHG_OK;
+}
+
 // Twiddle tables exp(-2 pi i m/N), N = 16..256, at [N, 2N) of the device symbol.
 int ensure_twiddles(int device) {
     static std::mutex mu;
@@ -209,6 +222,7 @@ class Batch {
         const size_t step_off = 6 * region;
         const size_t acc_off = step_off + al(nz_total * sizeof(float4));
         const size_t total = acc_off + al(4 * sizeof(double) * n);
+        SHG_TRY_INT(device_fits(total, "batch"));
         SHG_CUDA(cudaMalloc(&pool_, total));
         pool_bytes_ = total;
         acc_ = reinterpret_cast<double *>(pool_ + acc_off);
@@ -1310,7 +1324,10 @@ int shg_get_powers(shg_handle *h, double *p_pump_in, double *p_sh_out, double *p
     }
     if (h->th) return h->th->powers(p_pump_in, p_sh_out, p_pump_out);
     std::vector<double> acc;
-    SHG_CUDA(cudaDeviceSynchronize());
+    // the run was enqueued on the handle's stream (shg_run / shg_cwes) or the caller's
+    // (shg_cwes_device, which the caller orders before this call): waiting for the
+    // handle's stream leaves every other handle and stream on the device running
+    SHG_CUDA(cudaStreamSynchronize(h->stream));
     SHG_TRY(h->batch.copy_acc(acc));
     h->batch.powers_of(0, acc, p_pump_in, p_sh_out, p_pump_out);
     return SHG_OK;
@@ -1353,6 +1370,51 @@ int shg_grad_device(shg_handle *h, float temp, const void *pump_in, const void *
     if (!h->adj) h->adj.reset(new AdjointWork);
     return adjoint_run(h->cfg, h->batch.desc(0), h->batch.device_desc(), temp, checkpoints, *h->adj, st,
                        static_cast<float2 *>(grad_pump), static_cast<float2 *>(grad_sh), out4);
+}
+
+int shg_grad_run(shg_handle *h, float power, float waist, float focalpoint, float temp, const void *pump_factor,
+                 int checkpoints, void *grad_pump, double *out8, void *stream) {
+    SHG_TRY(check_handle(h));
+    if (h->th) {
+        set_error("shg_grad_run: gradients are for plain handles (hold the temperature field fixed)");
+        return SHG_ERR_STATE;
+    }
+    if (!out8) {
+        set_error("shg_grad_run: out8 is required");
+        return SHG_ERR_INVALID;
+    }
+    if (!(power > 0) || !(waist > 0) || !std::isfinite(focalpoint) || !std::isfinite(temp)) {
+        set_error("shg_grad_run: power and waist must be positive, focal point and temperature finite");
+        return SHG_ERR_INVALID;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // Solver.h:342-348: pump (setPump at Temp), propagators and delta-k at Temp, SH from zero
+    h->sp.power = power;
+    h->sp.waist = waist;
+    h->sp.focal = focalpoint;
+    h->sp.temp = temp;
+    h->sp.tpump = temp;
+    h->sp.tprop = temp;
+    h->pump_given = false;
+    h->sh_given = false;
+    h->have_pump = true;
+    SHG_TRY(h->batch.set_params(0, h->sp));
+    h->batch.set_slices(0, nullptr);
+    h->batch.set_sources(0, nullptr, nullptr);
+    SHG_TRY(h->batch.setup_only(st));
+    const InstDesc &d = h->batch.desc(0);
+    const float2 *factor = static_cast<const float2 *>(pump_factor);
+    if (factor) SHG_CUDA(launch_cmul_inplace(d.P, factor, h->n * h->n, st));
+    if (!h->adj) h->adj.reset(new AdjointWork);
+    SHG_TRY(adjoint_run(h->cfg, d, h->batch.device_desc(), temp, checkpoints, *h->adj, st,
+                        static_cast<float2 *>(grad_pump), nullptr, out8));
+    double pg[4];
+    SHG_TRY(pump_param_gradients(h->cfg, d, power, waist, focalpoint, temp, factor, *h->adj, st, pg));
+    out8[4] = pg[0];
+    out8[5] = pg[1];
+    out8[6] = pg[2];
+    out8[7] = out8[1] + pg[3];
+    return SHG_OK;
 }
 
 int shg_set_output_dir(shg_handle *h, const char *dir) {
@@ -1476,7 +1538,15 @@ int shg_batch_results(shg_batch *b, double *eta) {
     }
     std::vector<double> acc;
     SHG_TRY(b->batch.copy_acc(acc));
-    for (int i = 0; i < b->batch.size(); ++i) eta[i] = b->batch.eta_of(i, acc);
+    int bad = -1;
+    for (int i = 0; i < b->batch.size(); ++i) {
+        eta[i] = b->batch.eta_of(i, acc);
+        if (bad < 0 && !std::isfinite(eta[i])) bad = i;
+    }
+    if (bad >= 0) {
+        set_error("efficiency of solve " + std::to_string(bad) + " is not finite (every solve's value is stored)");
+        return SHG_ERR_NONFINITE;
+    }
     return SHG_OK;
 }
 

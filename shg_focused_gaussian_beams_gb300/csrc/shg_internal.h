@@ -42,8 +42,10 @@ struct HeatCoef;
 struct ThermDesc;
 cudaError_t launch_init_temperature(float *T, int nx, int ny, int nz, float temp, float t1, float t2, int bc,
                                     cudaStream_t st);
+// err: the caller's device error word, set to 1 by the TMA-staged sweep when one of its
+// bounded pipeline waits gives up (read and cleared with heat_tma_error).
 cudaError_t launch_heat(float *Tf, const float *Ti, const float *QK, const HeatCoef &c, int nx, int ny, int nz,
-                        int bc, cudaStream_t st);
+                        int bc, int *err, cudaStream_t st);
 // K = levels sweeps in one launch (temporal blocking), levels in {2, 3, 4}; bit-identical
 // to K launch_heat calls. heat_levels(): the level count in use (SHG_HEAT_TB, default 1 =
 // no temporal blocking: the sweep is issue-bound, and the blocked form's redundant halo
@@ -53,11 +55,14 @@ cudaError_t launch_heat_tb(float *Tf, const float *Ti, const float *QK, const He
 int heat_levels();
 cudaError_t verify_fast_division(float d, float r, unsigned long long *d_count, unsigned long long *mismatches,
                                  cudaStream_t st);
-// shg_heat_tma.cu: the TMA-staged sweep (NX % 4 == 0) and its pipeline error flag.
+// shg_heat_tma.cu: the TMA-staged sweep (NX % 4 == 0) and its pipeline error word. Each
+// THERMAL solve owns one device int; component calls lease one from a pool.
 bool heat_tma_supported(int nx, int ny, int nz);
 cudaError_t launch_heat_tma(float *Tf, const float *Ti, const float *QK, const HeatCoef &c, int nx, int ny, int nz,
-                            int bc, cudaStream_t st, int rows_per_warp = 1);
-cudaError_t heat_tma_error(int *flag, cudaStream_t st);
+                            int bc, int *err, cudaStream_t st, int rows_per_warp = 1);
+cudaError_t heat_tma_error(int *err, int *flag, cudaStream_t st);
+cudaError_t heat_error_word_acquire(int **err);
+void heat_error_word_release(int *err);
 cudaError_t launch_sq_diff_sum(const float *Tf, const float *Ti, size_t n, double *out, cudaStream_t st);
 cudaError_t launch_sq_sums(const float *Tf, const float *Ti, size_t n, double *out2, cudaStream_t st);
 cudaError_t launch_sellmeier_tables(const float *T, float *NP, float *NS, float *DK, size_t n, float lp, float ls,
@@ -85,5 +90,6 @@ float sellmeier(float L, float T);
 void fill_scalars(const shg_config &cr, const SolveParams &sp, InstDesc &d);
 double field_power(double sum_abs2, float n_index, float dx, float dy);
 int ensure_twiddles(int device);
+int device_fits(size_t bytes, const char *what);
 
 }  // namespace shg

@@ -19,7 +19,12 @@
 //
 // Set-up: the first call on a device, with that device current, looks up the array's
 // device address (cudaGetSymbolAddress) and uploads the FFT twiddle tables with a
-// blocking copy; make that first call before any stream capture.
+// blocking copy; make that first call before any stream capture. Both are cached per
+// device ordinal for the life of the process, so a device reset (cudaDeviceReset, or a
+// new primary context) after the first call is not supported.
+//
+// The call's own parameters (the solve descriptor) reach the device as a kernel argument
+// of a one-thread staging kernel, so no copy reads host memory after the call returns.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -68,6 +73,16 @@ int scratch_for(int dev, unsigned char **out) {
     }
     *out = g_scratch_addr[dev];
     return SHG_OK;
+}
+
+// Writes the solve descriptor and the one-entry solve list into the scratch array and
+// clears the power sums. The descriptor travels by value as a kernel argument.
+__global__ void k_noalloc_stage(InstDesc d, InstDesc *dst, int *list) {
+    if (threadIdx.x == 0) {
+        *dst = d;
+        list[0] = 0;
+        d.acc[0] = d.acc[1] = d.acc[2] = d.acc[3] = 0.0;
+    }
 }
 
 }  // namespace
@@ -126,14 +141,12 @@ extern "C" int shg_cwes_noalloc(const shg_config *cfg, float temp, const void *p
     d.Pout = static_cast<float2 *>(pump_out);
     d.Sout = static_cast<float2 *>(sh_out);
     d.pump_given = 1;
-    const int list0 = 0;
     InstDesc *d_desc = reinterpret_cast<InstDesc *>(base + kOffDesc);
     int *d_list = reinterpret_cast<int *>(base + kOffList);
     const size_t bytes = (size_t)n * n * sizeof(float2);
 
-    NOALLOC_CUDA(cudaMemcpyAsync(d_desc, &d, sizeof(d), cudaMemcpyHostToDevice, st));
-    NOALLOC_CUDA(cudaMemcpyAsync(d_list, &list0, sizeof(int), cudaMemcpyHostToDevice, st));
-    NOALLOC_CUDA(cudaMemsetAsync(d.acc, 0, 4 * sizeof(double), st));
+    k_noalloc_stage<<<1, 32, 0, st>>>(d, d_desc, d_list);
+    NOALLOC_CUDA(cudaGetLastError());
     NOALLOC_CUDA(cudaMemcpyAsync(d.P, pump_in, bytes, cudaMemcpyDeviceToDevice, st));
     if (sh_in)
         NOALLOC_CUDA(cudaMemcpyAsync(d.S, sh_in, bytes, cudaMemcpyDeviceToDevice, st));

@@ -665,13 +665,13 @@ cudaError_t launch_heat_tb(float *Tf, const float *Ti, const float *QK, const He
 // Measured at 256x256x400 on GB300, us per sweep: tma 70.0, tma2 76.1, tma1 92.6, tma8 78.0,
 // ws4 96.6, ws4b 100.0, ws8 178, 25 108.6.
 cudaError_t launch_heat(float *Tf, const float *Ti, const float *QK, const HeatCoef &c, int nx, int ny, int nz,
-                        int bc, cudaStream_t st) {
+                        int bc, int *err, cudaStream_t st) {
     const char *env = std::getenv("SHG_HEAT");
     std::string kind = env ? env : "tma";
     const bool fits32 = (long long)nx * ny * (nz + 3) < (1ll << 31);
     if (kind == "tma" || kind == "tma1" || kind == "tma2" || kind == "tma4" || kind == "tma8") {
         const int rows = kind == "tma" ? 4 : kind[3] - '0';
-        if (heat_tma_supported(nx, ny, nz)) return launch_heat_tma(Tf, Ti, QK, c, nx, ny, nz, bc, st, rows);
+        if (heat_tma_supported(nx, ny, nz)) return launch_heat_tma(Tf, Ti, QK, c, nx, ny, nz, bc, err, st, rows);
         kind = "ws4";
     }
     if (fits32 && (kind == "ws8" || kind == "ws4" || kind == "ws4b")) {

@@ -101,7 +101,12 @@ __device__ __forceinline__ void rk4_point_th(float2 &P, float2 &S, const ThCoef 
 // ---- one voxel of the heat stencil (shared by the sweep kernels) ----------------------
 
 // a / d for the interior stencil: the corrected product where it was verified equal to the
-// IEEE quotient, IEEE division otherwise.
+// IEEE quotient, IEEE division otherwise. The corrected product is the textbook FMA
+// quotient-correction step (P. Markstein, "Computation of elementary functions on the IBM
+// RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990): q = a * r with r = 1/d
+// rounded, the residual a - q*d formed exactly by one FMA, then q + residual * r. It is
+// not correctly rounded for every a, which is why verify_fast_division compares it with
+// IEEE division for every numerator of the exponent range used before it is enabled.
 __device__ __forceinline__ float div_const(float a, float d, float r, int fast) {
     const unsigned e = (__float_as_uint(a) >> 23) & 0xffu;
     if (fast && e - kDivExpLo <= kDivExpHi - kDivExpLo) {

@@ -147,12 +147,24 @@ int ThermalSolve::create(const shg_config &cfg) {
     return SHG_OK;
 }
 
-int ThermalSolve::sq_diff(float *out) {
-    double sum = 0.0;
-    TH_CUDA(launch_sq_diff_sum(T_cur(), T_prev(), tsize_, scratch_sum_, st_));
-    TH_CUDA(cudaMemcpyAsync(&sum, scratch_sum_, sizeof(double), cudaMemcpyDeviceToHost, st_));
+// Reports and clears a set error word (read beside the residual sums in `words`).
+int ThermalSolve::check_error_word(const double *words) {
+    int flag = 0;
+    std::memcpy(&flag, words, sizeof(int));
+    if (!flag) return SHG_OK;
+    TH_CUDA(cudaMemsetAsync(err_, 0, sizeof(int), st_));
     TH_CUDA(cudaStreamSynchronize(st_));
-    *out = (float)sum / (float)(unsigned)tsize_;
+    set_error("heat sweep: a TMA pipeline wait gave up (sweep incomplete)");
+    return SHG_ERR_CUDA;
+}
+
+int ThermalSolve::sq_diff(float *out) {
+    double w[3] = {0.0, 0.0, 0.0};  // residual sum, (unused), error word
+    TH_CUDA(launch_sq_diff_sum(T_cur(), T_prev(), tsize_, scratch_sum_, st_));
+    TH_CUDA(cudaMemcpyAsync(w, scratch_sum_, sizeof(w), cudaMemcpyDeviceToHost, st_));
+    TH_CUDA(cudaStreamSynchronize(st_));
+    TH_TRY(check_error_word(w + 2));
+    *out = (float)w[0] / (float)(unsigned)tsize_;
     return SHG_OK;
 }
 
@@ -168,18 +180,16 @@ int ThermalSolve::sweeps(float t_inf, int n) {
         cur_ ^= 1;
     }
     for (int k = 0; k < n; ++k) {
-        TH_CUDA(launch_heat(T_[cur_ ^ 1], T_[cur_], qk_, hc_, n_, n_, nz_, bc_, st_));
+        TH_CUDA(launch_heat(T_[cur_ ^ 1], T_[cur_], qk_, hc_, n_, n_, nz_, bc_, err_, st_));
         cur_ ^= 1;
     }
     return SHG_OK;
 }
 
-// Solver.h:302-324: the residual is checked after the first sweep and then after every
-// 5000th; the loop stops when it is below 5e-4/TSIZE or equal to the previous check.
-// A TMA-staged sweep whose pipeline gave up leaves its error flag set: report it.
-static int heat_pipeline_ok(cudaStream_t st) {
+// A TMA-staged sweep whose pipeline gave up leaves its error word set: report it.
+static int heat_pipeline_ok(int *err, cudaStream_t st) {
     int flag = 0;
-    TH_CUDA(heat_tma_error(&flag, st));
+    TH_CUDA(heat_tma_error(err, &flag, st));
     if (flag) {
         set_error("heat sweep: a TMA pipeline wait gave up (sweep incomplete)");
         return SHG_ERR_CUDA;
@@ -187,17 +197,26 @@ static int heat_pipeline_ok(cudaStream_t st) {
     return SHG_OK;
 }
 
+int ThermalSolve::sweeps_checked(float t_inf, int n) {
+    TH_TRY(sweeps(t_inf, n));
+    return heat_pipeline_ok(err_, st_);
+}
+
+// Solver.h:302-324: the residual is checked after the first sweep and then after every
+// 5000th; the loop stops when it is below 5e-4/TSIZE or equal to the previous check. The
+// error word is read at every residual check, so a sweep whose pipeline gave up ends the
+// solve there (its stale voxels could otherwise keep the residual above the tolerance).
 int ThermalSolve::jacobi(float t_inf, int *counter) {
     const int rc = jacobi_run(t_inf, counter);
     if (rc) return rc;
-    return heat_pipeline_ok(st_);
+    return heat_pipeline_ok(err_, st_);
 }
 
 int ThermalSolve::jacobi_run(float t_inf, int *counter) {
     if (rel_tol_ > 0) {
         // relative residual of one sweep, every check_every sweeps
         int c = 0;
-        double sums[2];
+        double sums[3];  // |T_k+1 - T_k|^2, |T_k+1|^2, error word
         for (;;) {
             const int n = std::min(check_every_ - 1, max_sweeps_ - 1 - c);
             if (n > 0) TH_TRY(sweeps(t_inf, n));
@@ -206,6 +225,7 @@ int ThermalSolve::jacobi_run(float t_inf, int *counter) {
             TH_CUDA(launch_sq_sums(T_cur(), T_prev(), tsize_, scratch_sum_, st_));
             TH_CUDA(cudaMemcpyAsync(sums, scratch_sum_, sizeof(sums), cudaMemcpyDeviceToHost, st_));
             TH_CUDA(cudaStreamSynchronize(st_));
+            TH_TRY(check_error_word(sums + 2));
             last_rel_ = sums[1] > 0 ? std::sqrt(sums[0] / sums[1]) : 0.0;
             if (last_rel_ < rel_tol_ || c >= max_sweeps_) break;
         }
@@ -418,8 +438,7 @@ int shg_heat_sweeps(const shg_config *cfg, float *T_inout, const float *Q, float
     TH_CUDA(cudaMemcpy(ts.QK(), qk.data(), n * sizeof(float), cudaMemcpyHostToDevice));
     TH_CUDA(cudaMemcpy(ts.T_cur(), T_inout, n * sizeof(float), cudaMemcpyHostToDevice));
     TH_CUDA(cudaMemcpy(ts.T_prev(), T_inout, n * sizeof(float), cudaMemcpyHostToDevice));
-    TH_TRY(ts.sweeps(t_inf, nsweeps));
-    TH_TRY(heat_pipeline_ok(ts.stream()));
+    TH_TRY(ts.sweeps_checked(t_inf, nsweeps));
     return ts.copy_temperature(T_inout);
 }
 
@@ -433,6 +452,13 @@ int shg_heat_sweeps_device(const shg_config *cfg, void *Ta, void *Tb, const void
     HeatCoef hc = make_heat_coef(*cfg, t_inf);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     TH_TRY(enable_fast_division(hc, st));
+    // this call's own error word, leased from a pool (no other call can set or clear it)
+    int *err = nullptr;
+    TH_CUDA(heat_error_word_acquire(&err));
+    struct Lease {
+        int *w;
+        ~Lease() { heat_error_word_release(w); }
+    } lease{err};
     float *a = static_cast<float *>(Ta), *b = static_cast<float *>(Tb);
     const int L = heat_levels();
     for (; L > 1 && nsweeps >= L; nsweeps -= L) {
@@ -440,10 +466,11 @@ int shg_heat_sweeps_device(const shg_config *cfg, void *Ta, void *Tb, const void
         std::swap(a, b);
     }
     for (int k = 0; k < nsweeps; ++k) {
-        TH_CUDA(launch_heat(b, a, static_cast<const float *>(QK), hc, cfg->nx, cfg->ny, cfg->nz, bc, st));
+        TH_CUDA(launch_heat(b, a, static_cast<const float *>(QK), hc, cfg->nx, cfg->ny, cfg->nz, bc, err, st));
         std::swap(a, b);
     }
-    return heat_pipeline_ok(st);
+    // heat_pipeline_ok synchronises `st` and clears the word before it returns to the pool
+    return heat_pipeline_ok(err, st);
 }
 
 int shg_dk_thermal(const shg_config *cfg, const float *T, float *DK, float *NP, float *NS) {

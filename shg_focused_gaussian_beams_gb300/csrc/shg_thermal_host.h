@@ -47,6 +47,7 @@ class ThermalSolve {
     }
     double last_residual() const { return last_rel_; }
     int sweeps(float t_inf, int n);          // n plain sweeps
+    int sweeps_checked(float t_inf, int n);  // n sweeps, then the pipeline error word checked
     int cwes(float power, float waist, float focal);  // one thermal CWES from the current T
 
     // Indices and delta-k of the current T (PhaseMatching.h:41-54), the centre temperature
@@ -68,6 +69,7 @@ class ThermalSolve {
 
    private:
     int sq_diff(float *out);
+    int check_error_word(const double *words);
     int jacobi_run(float t_inf, int *counter);
     shg_config cfg_{};
     int n_ = 0, nz_ = 0, bc_ = 0;
@@ -78,6 +80,7 @@ class ThermalSolve {
     float2 *f_ = nullptr;   // P, S, Pout, Sout, Hp, Hs
     float4 *stepc_ = nullptr;
     double *acc_ = nullptr, *scratch_sum_ = nullptr;
+    int *err_ = nullptr;  // heat-sweep error word of this solve (in acc_)
     InstDesc *d_desc_ = nullptr;
     InstDesc h_desc_{};
     ThermDesc th_{};

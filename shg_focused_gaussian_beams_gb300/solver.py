@@ -124,6 +124,23 @@ class Solver:
                                     int(checkpoints), gp.data_ptr(), gs.data_ptr(), out, st), "shg_grad_device")
         return {"loss": out[0], "grad_pump": gp, "grad_sh": gs, "dT": out[1], "dLambda": out[2], "ddk": out[3]}
 
+    def grad_run(self, power, waist, focalpoint, temp, pump_factor=None, checkpoints=20, stream=None, device=None):
+        """Adjoint pass of Solver::run's plain path (Gaussian pump of setPump at `temp`, times
+        the optional complex64 CUDA tensor pump_factor; SH from zero): L = SH output power and
+        its gradients with respect to the input pump field, the oven temperature (input field
+        held fixed, and in total through the pump's index), the poling period, the focal
+        point, the waist and the pump power. Returns a dict."""
+        import torch
+        dev = pump_factor.device if pump_factor is not None else torch.device(device or f"cuda:{self.cfg.device}")
+        gp = torch.empty((self.ny, self.nx), dtype=torch.complex64, device=dev)
+        out = (C.c_double * 8)()
+        st = torch.cuda.current_stream(dev).cuda_stream if stream is None else stream
+        fac = None if pump_factor is None else pump_factor.contiguous().data_ptr()
+        check(lib().shg_grad_run(self._h, power, waist, focalpoint, temp, fac, int(checkpoints), gp.data_ptr(), out,
+                                 st), "shg_grad_run")
+        return {"loss": out[0], "grad_pump": gp, "dT": out[1], "dLambda": out[2], "ddk": out[3], "dfocal": out[4],
+                "dwaist": out[5], "dpower": out[6], "dT_total": out[7]}
+
     def fields(self):
         p = np.zeros((self.ny, self.nx), np.complex64)
         s = np.zeros((self.ny, self.nx), np.complex64)
@@ -221,6 +238,11 @@ class Sweep:
         sh = [(it.ny, it.nx) for it in self.instances]
         return ([p[off[i]:off[i + 1]].reshape(sh[i]) for i in range(self.n)],
                 [s[off[i]:off[i + 1]].reshape(sh[i]) for i in range(self.n)])
+
+    def pump_fields_into(self, ptr):
+        """Copy the output pump fields of every solve (contiguous, solve order) to a
+        caller-owned host buffer at address ptr (e.g. pinned memory)."""
+        check(lib().shg_batch_fields(self._b, C.c_void_p(ptr), None), "shg_batch_fields")
 
     def set_instances(self, instances):
         arr = (_lib.Instance * self.n)()

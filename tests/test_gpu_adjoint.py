@@ -225,6 +225,55 @@ def test_autograd_focus_and_temperature(case):
     assert abs(temp.grad.item() - case["r"]["dT"]) / abs(case["r"]["dT"]) < 1e-6
 
 
+def _loss_params64(c, power, waist, focal, T, pert):
+    """FP64 loss of Solver::run's plain path for the pump of (power, waist, focal) at index
+    temperature T times the fixed perturbation; delta-k follows T as in loss64."""
+    o = c["o"]
+    return loss64(c, o.set_pump64(power, focal, waist, T) * pert, T=T)
+
+
+def test_grad_run_pump_parameters_vs_fd(case):
+    """shg_grad_run (Gaussian pump of setPump built on the device, times the seeded
+    perturbation): focal point, waist, power and the total temperature derivative (the pump's
+    index follows T too) against FP64 central differences; the pump-gradient field and the
+    fixed-field derivatives equal those of shg_grad_device on the same input."""
+    inst = case["inst"]
+    pert = case["pert"]
+    s = case["s"]
+    fac = torch.from_numpy(pert.astype(np.complex64)).cuda()
+    r = s.grad_run(inst.power, inst.waist, inst.focal, T0, pump_factor=fac, checkpoints=7)
+    f0, w0, p0 = float(np.float32(inst.focal)), float(np.float32(inst.waist)), float(np.float32(inst.power))
+    checks = [("dfocal", 1e-4 * f0, lambda h: _loss_params64(case, p0, w0, f0 + h, T0, pert)),
+              ("dwaist", 1e-4 * w0, lambda h: _loss_params64(case, p0, w0 + h, f0, T0, pert)),
+              ("dpower", 1e-4 * p0, lambda h: _loss_params64(case, p0 + h, w0, f0, T0, pert)),
+              ("dT_total", 1e-4 * T0, lambda h: _loss_params64(case, p0, w0, f0, T0 + h, pert))]
+    for key, h, fn in checks:
+        fd = (fn(h) - fn(-h)) / (2 * h)
+        assert abs(r[key] - fd) / abs(fd) < FD_RTOL, (key, r[key], fd)
+    # the same input through shg_grad_device: pump built on the device equals the float pump
+    pump32 = (case["o"].set_pump(inst.power, inst.focal, inst.waist, T0) * pert).astype(np.complex64)
+    r2 = s.grad(T0, torch.from_numpy(pump32).cuda(), checkpoints=7)
+    g1, g2 = r["grad_pump"].cpu().numpy(), r2["grad_pump"].cpu().numpy()
+    assert np.linalg.norm(g1 - g2) / np.linalg.norm(g2) < 1e-5
+    assert abs(r["dT"] - r2["dT"]) / abs(r2["dT"]) < 1e-5
+    assert abs(r["loss"] - r2["loss"]) / r2["loss"] < 1e-6
+
+
+def test_run_power_autograd_uses_the_c_abi_gradients(case):
+    """autograd.run_power back-propagates the C ABI's pump-parameter gradients."""
+    from shg_focused_gaussian_beams_gb300.autograd import run_power
+    inst = case["inst"]
+    fac = torch.from_numpy(case["pert"].astype(np.complex64)).cuda()
+    args = [torch.tensor(v, dtype=torch.float64, device="cuda", requires_grad=True)
+            for v in (inst.power, inst.waist, inst.focal, T0, case["cfg"].lambda_qpm)]
+    L = run_power(case["s"], *args, pump_factor=fac, checkpoints=7)
+    L.backward()
+    r = case["s"].grad_run(inst.power, inst.waist, inst.focal, T0, pump_factor=fac, checkpoints=7)
+    for t, key in zip(args, ("dpower", "dwaist", "dfocal", "dT_total", "dLambda")):
+        assert abs(t.grad.item() - r[key]) <= 1e-9 * abs(r[key]), key
+    assert abs(L.item() - r["loss"]) <= 1e-12 * r["loss"]
+
+
 def _fd_job(args):
     """One FP64 loss evaluation of the full-size case in a separate process."""
     import oracle as Ox
@@ -237,17 +286,20 @@ def _fd_job(args):
 def test_config_adjoint_256x400_full_size():
     """The adjoint workload at full size: 256x256x400, P = 20 W, xi = 2.84, Gaussian pump
     times a seeded 5 % perturbation smooth over 8 cells, 20 checkpoints; FP64 central
-    differences (run in parallel processes) on 32 seeded field directions, T and Lambda, as the
-    adjoint workload specifies."""
+    differences (run in parallel processes) on 32 seeded field directions, T, Lambda and the
+    focus position (through shg_grad_run), as the adjoint workload specifies."""
     import multiprocessing as mpx
     n, nz = 256, 400
     inst = W.plain_instance(n, nz, 20.0, 2.84, T0)
     cfg = O.make_cfg(W.CRYSTAL_QPM50, n, n, nz, inst.lx, inst.ly)
     o = O.Oracle(cfg)
     rng = np.random.default_rng(12)
-    pump = o.set_pump64(inst.power, inst.focal, inst.waist, T0) * (1 + 0.05 * smooth_noise(rng, n))
+    pert = 1 + 0.05 * smooth_noise(rng, n)
+    pump = o.set_pump64(inst.power, inst.focal, inst.waist, T0) * pert
     s = Solver(crystal=W.CRYSTAL_QPM50, nx=n, ny=n, nz=nz, lx=inst.lx, ly=inst.ly)
     r = s.grad(T0, torch.from_numpy(pump.astype(np.complex64)).cuda(), checkpoints=20)
+    rr = s.grad_run(inst.power, inst.waist, inst.focal, T0, checkpoints=20,
+                    pump_factor=torch.from_numpy(pert.astype(np.complex64)).cuda())
     g = r["grad_pump"].cpu().numpy().astype(np.complex128)
     dk32 = float(o.dk_constant(T0))
     lam = cfg.lambda_qpm
@@ -269,6 +321,11 @@ def test_config_adjoint_256x400_full_size():
     for sgn in (1, -1):
         jobs.append((cfg_t, pump, T0, dk32 + 2 * math.pi * (1.0 / (lam + sgn * hL) - 1.0 / lam)))
     meta.append(("L", 2 * hL, None))
+    # focus position: the Gaussian of setPump moved by +-h, the same perturbation
+    hf = 1e-4 * inst.focal
+    for sgn in (1, -1):
+        jobs.append((cfg_t, o.set_pump64(inst.power, inst.focal + sgn * hf, inst.waist, T0) * pert, T0, dk32))
+    meta.append(("f", 2 * hf, None))
     with mpx.get_context("spawn").Pool(min(len(jobs), os.cpu_count() or 1)) as pool:
         vals = [kl * v for v in pool.map(_fd_job, jobs)]
     adj, fd = [], []
@@ -279,6 +336,8 @@ def test_config_adjoint_256x400_full_size():
             fd.append(fdk)
         elif kind == "T":
             assert abs(r["dT"] - fdk) / abs(fdk) < FD_RTOL, (r["dT"], fdk)
+        elif kind == "f":
+            assert abs(rr["dfocal"] - fdk) / abs(fdk) < FD_RTOL, (rr["dfocal"], fdk)
         else:
             assert abs(r["dLambda"] - fdk) / abs(fdk) < FD_RTOL, (r["dLambda"], fdk)
     adj, fd = np.array(adj), np.array(fd)
