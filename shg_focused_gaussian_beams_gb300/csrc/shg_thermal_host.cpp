@@ -139,11 +139,14 @@ int ThermalSolve::create(const shg_config &cfg) {
     TH_CUDA(cudaMalloc(&dkint_, nn * sizeof(float)));
     TH_CUDA(cudaMalloc(&f_, 6 * nn * sizeof(float2)));
     TH_CUDA(cudaMalloc(&stepc_, (size_t)nz_ * sizeof(float4)));
-    TH_CUDA(cudaMalloc(&acc_, 8 * sizeof(double)));  // [0..3] power sums, [4] list entry, [5..6] residual sums
+    // [0..3] power sums, [4] list entry, [5..6] residual sums, [7] the heat-sweep error word
+    // (an int, set by a TMA pipeline wait that gave up; read with the residual sums)
+    TH_CUDA(cudaMalloc(&acc_, 8 * sizeof(double)));
     TH_CUDA(cudaMalloc(&d_desc_, sizeof(InstDesc)));
     TH_CUDA(cudaMemset(qk_, 0, tsize_ * sizeof(float)));
     TH_CUDA(cudaMemset(acc_, 0, 8 * sizeof(double)));
     scratch_sum_ = acc_ + 5;
+    err_ = reinterpret_cast<int *>(acc_ + 7);
     return SHG_OK;
 }
 

@@ -77,10 +77,10 @@ def test_batch_past_free_memory_is_refused_on_the_host():
 def test_starved_heat_pipeline_ends_the_jacobi_solve_promptly(rule, monkeypatch):
     monkeypatch.setenv("SHG_HEAT", "tma")
     monkeypatch.setenv("SHG_HEAT_TB", "1")
-    inst = W.plain_instance(40, 24, 20.0, 2.84, 50.0)
-    s = S.Solver(crystal=W.CRYSTAL_QPM50, nx=40, ny=40, nz=24, lx=inst.lx, ly=inst.ly, thermal=True, bc=1)
+    inst = W.plain_instance(32, 24, 20.0, 2.84, 50.0)
+    s = S.Solver(crystal=W.CRYSTAL_QPM50, nx=32, ny=32, nz=24, lx=inst.lx, ly=inst.ly, thermal=True, bc=1)
     if rule == "relative":
-        s.set_jacobi_rule(1e-9, check_every=20, max_sweeps=100000)
+        s.set_jacobi_rule(1e-9, check_every=5, max_sweeps=100000)
     monkeypatch.setenv("SHG_HEAT_TMA_STARVE", "1")
     t0 = time.time()
     with pytest.raises(ShgError, match="TMA pipeline wait gave up"):
@@ -90,9 +90,9 @@ def test_starved_heat_pipeline_ends_the_jacobi_solve_promptly(rule, monkeypatch)
     assert time.time() - t0 < 60
     monkeypatch.delenv("SHG_HEAT_TMA_STARVE")
     s.run(20.0, inst.waist, inst.focal, 50.0, 25.0, 50.0, 50.0)
-    ref = S.Solver(crystal=W.CRYSTAL_QPM50, nx=40, ny=40, nz=24, lx=inst.lx, ly=inst.ly, thermal=True, bc=1)
+    ref = S.Solver(crystal=W.CRYSTAL_QPM50, nx=32, ny=32, nz=24, lx=inst.lx, ly=inst.ly, thermal=True, bc=1)
     if rule == "relative":
-        ref.set_jacobi_rule(1e-9, check_every=20, max_sweeps=100000)
+        ref.set_jacobi_rule(1e-9, check_every=5, max_sweeps=100000)
     ref.run(20.0, inst.waist, inst.focal, 50.0, 25.0, 50.0, 50.0)
     assert bits_equal(s.temperature(), ref.temperature())
     assert s.jacobi_counts() == ref.jacobi_counts()

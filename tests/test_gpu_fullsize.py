@@ -8,8 +8,12 @@
 * The 512-solve sweep: the first solve of each of the nine (N, Nz) classes at its full
   length, batched on the device, against the FP32 restatement and the FP64 run.
 
-Bar: output fields within relative L2 1e-4 and conversion efficiency within 1e-4 relative;
-bit-identity where the reference's float arithmetic is reproduced exactly.
+Bar: output fields within relative L2 1e-4 and conversion efficiency within 1e-4 relative
+of the FP32 restatement (the reference's arithmetic); bit-identity where the reference's
+float arithmetic is reproduced exactly. Against the FP64 run the reference's own FP32
+arithmetic already differs by up to ~2.5e-4 on some solves (FFT rounding over 400 slices,
+and efficiencies far from phase matching), so there the bar is 1e-4 or 1.5 times the
+reference's own FP32-to-FP64 distance on the same solve, whichever is larger.
 """
 import concurrent.futures as cf
 import os
@@ -105,12 +109,12 @@ def test_thermal256_fixed_temperature_cwes(thermal256):
         po64, so64 = f64.result()
     assert rel_l2(dev["sh"], so) < FIELD_RTOL
     assert rel_l2(dev["pump"], po) < FIELD_RTOL
-    assert rel_l2(dev["sh"], so64) < FIELD_RTOL
-    assert rel_l2(dev["pump"], po64) < FIELD_RTOL
     e32 = eta(pump, so, o.n(1.064, tc), o.n(np.float32(0.532), tc))
     e64 = eta(pump64, so64, o.n64(1.064, tc), o.n64(0.532, tc))
     assert abs(dev["eta"] - e32) / e32 < ETA_RTOL
-    assert abs(dev["eta"] - e64) / e64 < ETA_RTOL
+    assert rel_l2(dev["sh"], so64) < fp64_bar(rel_l2(so, so64))
+    assert rel_l2(dev["pump"], po64) < fp64_bar(rel_l2(po, po64))
+    assert abs(dev["eta"] - e64) / e64 < fp64_bar(abs(e32 - e64) / e64)
 
 
 def _class_representatives():
@@ -122,6 +126,11 @@ def _class_representatives():
     return [pick[k] for k in sorted(pick)]
 
 
+def fp64_bar(d32):
+    """Bar against the FP64 run: 1e-4, or 1.5 x the reference arithmetic's own distance."""
+    return max(FIELD_RTOL, 1.5 * d32)
+
+
 def _oracle_solve(inst):
     o = O.Oracle(O.make_cfg(W.CRYSTAL_QPM50, inst.nx, inst.ny, inst.nz, inst.lx, inst.ly))
     pump = o.set_pump(inst.power, inst.focal, inst.waist, inst.temp)
@@ -130,7 +139,8 @@ def _oracle_solve(inst):
     po64, so64, _, _ = o.cwes_plain64(pump64, np.zeros_like(pump64), inst.temp, float(o.dk_constant(inst.temp)))
     e32 = eta(pump, so, o.n(1.064, inst.temp), o.n(np.float32(0.532), inst.temp))
     e64 = eta(pump64, so64, o.n64(1.064, inst.temp), o.n64(0.532, inst.temp))
-    return dict(po=po, so=so, po64=po64, so64=so64, e32=e32, e64=e64)
+    return dict(po=po, so=so, po64=po64, so64=so64, e32=e32, e64=e64, d_so=rel_l2(so, so64),
+                d_e=abs(e32 - e64) / e64)
 
 
 def test_sweep512_every_class_full_length():
@@ -147,7 +157,7 @@ def test_sweep512_every_class_full_length():
         tag = (inst.nx, inst.nz)
         assert rel_l2(shs[k], r["so"]) < FIELD_RTOL, tag
         assert rel_l2(pumps[k], r["po"]) < FIELD_RTOL, tag
-        assert rel_l2(shs[k], r["so64"]) < FIELD_RTOL, tag
         assert abs(eta_gpu[k] - r["e32"]) / r["e32"] < ETA_RTOL, tag
-        assert abs(eta_gpu[k] - r["e64"]) / r["e64"] < ETA_RTOL, tag
+        assert rel_l2(shs[k], r["so64"]) < fp64_bar(r["d_so"]), (tag, rel_l2(shs[k], r["so64"]), r["d_so"])
+        assert abs(eta_gpu[k] - r["e64"]) / r["e64"] < fp64_bar(r["d_e"]), (tag, eta_gpu[k], r["e64"], r["d_e"])
     sw.close()
