@@ -39,11 +39,24 @@ typedef struct shg_config {
     int bc;                  /* 0 = open top, bottom ovens (Tfield.h:113); 1 = oven surrounded (Tfield.h:224) */
     int sh_seed;             /* < 0: SH starts at zero; >= 0: seeded N(0, 1e-20) (Efields.h:129-144) */
     int device;              /* CUDA device ordinal */
+    int crystal;             /* refractive index n(L, T): SHG_CRYSTAL_SPPLT (Crystal.h:55-71) or
+                              * SHG_CRYSTAL_PPLN (README.md:48-49; see shg_index) */
 } shg_config;
+
+#define SHG_CRYSTAL_SPPLT 0  /* MgO:sPPLT, Bruner et al. Sellmeier: the reference's n(L, T) */
+#define SHG_CRYSTAL_PPLN 1   /* PPLN: congruent LiNbO3, Jundt, Opt. Lett. 22, 1553 (1997) */
 
 /* Fills `cfg` with the reference's compiled-in values (64x64x200 grid, 2000x1000x30000 um
  * MgO:sPPLT crystal, Crystal.h:26-53), thermal off, open-top BC, zero SH start, device 0. */
 int shg_config_init(shg_config *cfg);
+
+/* n(L, T) of Crystal.h:55-71 (extraordinary index at wavelength lambda_um [um] and
+ * temperature temp_c [C]) for the crystal SHG_CRYSTAL_SPPLT (the reference's Bruner et al.
+ * Sellmeier, bit-identical) or SHG_CRYSTAL_PPLN (periodically poled lithium niobate: the
+ * temperature-dependent Sellmeier fit of congruent LiNbO3 by D. H. Jundt, Opt. Lett. 22,
+ * 1553-1555 (1997); the reference's README names an MgO:PPLN crystal but its code has no
+ * routine for it). Both are evaluated in double and rounded to float. */
+int shg_index(int crystal, float lambda_um, float temp_c, float *n);
 
 typedef struct shg_handle shg_handle;
 

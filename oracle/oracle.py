@@ -21,7 +21,7 @@ _pf, _pd, _pi = C.POINTER(C.c_float), C.POINTER(C.c_double), C.POINTER(C.c_int)
 class Cfg(C.Structure):
     _fields_ = [("nx", _i), ("ny", _i), ("nz", _i), ("lx", _f), ("ly", _f), ("lz", _f), ("lp", _f),
                 ("deff", _f), ("lambda_qpm", _f), ("alpha_p", _f), ("alpha_s", _f), ("beta_s", _f),
-                ("rho_p", _f), ("rho_s", _f), ("kth", _f), ("htc", _f)]
+                ("rho_p", _f), ("rho_s", _f), ("kth", _f), ("htc", _f), ("crystal", _i)]
 
 
 class Inst(C.Structure):
@@ -43,6 +43,10 @@ def lib():
         L.oracle_n_f32.argtypes = [_f, _f]
         L.oracle_n_f64.restype = _d
         L.oracle_n_f64.argtypes = [_d, _d]
+        L.oracle_index_f32.restype = _f
+        L.oracle_index_f32.argtypes = [_i, _f, _f]
+        L.oracle_index_f64.restype = _d
+        L.oracle_index_f64.argtypes = [_i, _d, _d]
         P = C.POINTER(Cfg)
         L.oracle_set_pump_f32.argtypes = [P, _f, _f, _f, _f, _pf]
         L.oracle_set_pump_f64.argtypes = [P, _d, _d, _d, _d, _pd]
@@ -94,7 +98,7 @@ def make_cfg(crystal, nx, ny, nz, lx=None, ly=None) -> Cfg:
     g = crystal if isinstance(crystal, dict) else crystal.__dict__
     return Cfg(nx, ny, nz, g["lx"] if lx is None else lx, g["ly"] if ly is None else ly, g["lz"], g["lp"],
                g["deff"], g["lambda_qpm"], g["alpha_p"], g["alpha_s"], g["beta_s"], g["rho_p"], g["rho_s"],
-               g["kth"], g["htc"])
+               g["kth"], g["htc"], int(g.get("crystal", 0)))
 
 
 class Oracle:
@@ -108,12 +112,12 @@ class Oracle:
     def _c2(self, dt=np.complex64):
         return np.zeros((self.ny, self.nx), dt)
 
-    # Crystal.h:116
+    # Crystal.h:116 (or the PPLN fit for crystal 1)
     def n(self, L, T):
-        return np.float32(self.L.oracle_n_f32(L, T))
+        return np.float32(self.L.oracle_index_f32(self.cfg.crystal, L, T))
 
     def n64(self, L, T):
-        return float(self.L.oracle_n_f64(L, T))
+        return float(self.L.oracle_index_f64(self.cfg.crystal, L, T))
 
     def set_pump(self, power, focal, waist, tc):
         a = self._c2()

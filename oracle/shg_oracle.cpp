@@ -74,10 +74,31 @@ R sellmeier(R L, R T) {
     return (R)std::sqrt(n2);
 }
 
+// PPLN (congruent LiNbO3) extraordinary index, the fit of D. H. Jundt, Opt. Lett. 22,
+// 1553-1555 (1997): n^2 = a1 + b1 f + (a2 + b2 f)/(L^2 - (a3 + b3 f)^2) + (a4 + b4 f)/(L^2 - a5^2)
+// - a6 L^2, f = (T - 24.5)(T + 570.82); double, rounded to R. Not part of the reference's code
+// (its README names an MgO:PPLN crystal): a restatement of the published fit, evaluated in
+// the same operation order as the device code.
+template <class R>
+R lithium_niobate(R L, R T) {
+    const D a1 = 5.35583, a2 = 0.100473, a3 = 0.20692, a4 = 100.0, a5 = 11.34927, a6 = 1.5334e-2;
+    const D b1 = 4.629e-7, b2 = 3.862e-8, b3 = -0.89e-8, b4 = 2.657e-5;
+    const D t = (D)T, L2 = (D)L * (D)L;
+    const D f = (t - 24.5) * (t + 570.82);
+    const D c3 = a3 + b3 * f;
+    const D n2 = a1 + b1 * f + (a2 + b2 * f) / (L2 - c3 * c3) + (a4 + b4 * f) / (L2 - a5 * a5) - a6 * L2;
+    return (R)std::sqrt(n2);
+}
+
+template <class R>
+R crystal_n(int crystal, R L, R T) {
+    return crystal == 1 ? lithium_niobate<R>(L, T) : sellmeier<R>(L, T);
+}
+
 // Crystal.h:80-82 and the per-configuration constants of Crystal.h:26-53.
 template <class R>
 struct Model {
-    int NX, NY, NZ;
+    int NX, NY, NZ, crystal;
     size_t NXY, TSIZE;
     R PI, Cl, EPS0, lp, ls, LX, LY, LZ, dx, dy, dz, deff, dQ, Lambda, alpha_crp, alpha_crs, beta_crs,
         rhop, rhos, thermal_cond, heat_trf_coeff;
@@ -86,6 +107,7 @@ struct Model {
         NX = c.nx;
         NY = c.ny;
         NZ = c.nz;
+        crystal = c.crystal;
         NXY = (size_t)NX * NY;
         TSIZE = NXY * (size_t)NZ;
         PI = (R)3.14159265358979323846;
@@ -111,7 +133,7 @@ struct Model {
         heat_trf_coeff = (R)c.htc;
     }
     size_t idx(int x, int y, int z) const { return (size_t)z * NXY + (size_t)y * NX + x; }
-    R n(R L, R T) const { return sellmeier<R>(L, T); }
+    R n(R L, R T) const { return crystal_n<R>(crystal, L, T); }
 };
 
 template <class R>
@@ -575,6 +597,8 @@ extern "C" {
 
 float oracle_n_f32(float L, float T) { return sellmeier<float>(L, T); }
 double oracle_n_f64(double L, double T) { return sellmeier<double>(L, T); }
+float oracle_index_f32(int crystal, float L, float T) { return crystal_n<float>(crystal, L, T); }
+double oracle_index_f64(int crystal, double L, double T) { return crystal_n<double>(crystal, L, T); }
 
 void oracle_set_pump_f32(const oracle_cfg *c, float power, float focal, float waist, float tc, float *pump) {
     Model<float> m(*c);

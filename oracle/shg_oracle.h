@@ -32,11 +32,16 @@ typedef struct oracle_cfg {
     float alpha_p, alpha_s, beta_s;  /* Crystal.h:44-46 */
     float rho_p, rho_s; /* Crystal.h:47-48 */
     float kth, htc;     /* Crystal.h:52-53 */
+    int crystal;        /* 0: Crystal.h:55-71 (MgO:sPPLT); 1: PPLN, congruent LiNbO3 (Jundt 1997,
+                           not in the reference's code) */
 } oracle_cfg;
 
 /* Crystal.h:116-132 */
 float oracle_n_f32(float L, float T);
 double oracle_n_f64(double L, double T);
+/* n(L, T) of crystal 0 (the above) or 1 (PPLN: congruent LiNbO3, Jundt, Opt. Lett. 22, 1553 (1997)). */
+float oracle_index_f32(int crystal, float L, float T);
+double oracle_index_f64(int crystal, double L, double T);
 
 /* Efields.h:74-104 (pump), Efields.h:107-126 + 32-71 (shifted propagators), FP32. */
 void oracle_set_pump_f32(const oracle_cfg *c, float power, float focal, float waist, float tc, float *pump);

@@ -29,7 +29,7 @@ class Config(C.Structure):
     _fields_ = [("nx", _i), ("ny", _i), ("nz", _i), ("lx", _f), ("ly", _f), ("lz", _f), ("lp", _f),
                 ("deff", _f), ("lambda_qpm", _f), ("alpha_p", _f), ("alpha_s", _f), ("beta_s", _f),
                 ("rho_p", _f), ("rho_s", _f), ("kth", _f), ("htc", _f), ("thermal", _i), ("bc", _i),
-                ("sh_seed", _i), ("device", _i)]
+                ("sh_seed", _i), ("device", _i), ("crystal", _i)]
 
 
 class KernelStat(C.Structure):
@@ -44,6 +44,7 @@ class Instance(C.Structure):
 # name -> (restype, argtypes)
 SIGNATURES = {
     "shg_config_init": (_i, [C.POINTER(Config)]),
+    "shg_index": (_i, [_i, _f, _f, _pf]),
     "shg_create": (_i, [C.POINTER(Config), C.POINTER(_vp)]),
     "shg_destroy": (_i, [_vp]),
     "shg_run": (_i, [_vp, _f, _f, _f, _f, _f, _f, _f, _i, _i]),

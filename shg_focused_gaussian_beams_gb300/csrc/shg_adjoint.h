@@ -61,5 +61,6 @@ int adjoint_run(const shg_config &cfg, const InstDesc &h, const InstDesc *d, flo
 int pump_param_gradients(const shg_config &cfg, const InstDesc &h, float power, float waist, float focal, float temp,
                          const float2 *factor, AdjointWork &w, cudaStream_t st, double *out4);
 double sellmeier_dT(double L, double T);
+double crystal_index_dT(int crystal, double L, double T);
 
 }  // namespace shg

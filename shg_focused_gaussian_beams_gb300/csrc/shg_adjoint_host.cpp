@@ -86,6 +86,21 @@ int AdjointWork::ensure(int n_, int K_, int L_, int nck_) {
     return SHG_OK;
 }
 
+// dn/dT of the crystal's index in double (the smooth model behind the float index):
+// Crystal.h:116-132 (MgO:sPPLT) or the LiNbO3 fit of sellmeier_ln (PPLN).
+double crystal_index_dT(int crystal, double L, double T) {
+    if (crystal == SHG_CRYSTAL_PPLN) {
+        const double a1 = 5.35583, a2 = 0.100473, a3 = 0.20692, a4 = 100.0, a5 = 11.34927, a6 = 1.5334e-2;
+        const double b1 = 4.629e-7, b2 = 3.862e-8, b3 = -0.89e-8, b4 = 2.657e-5;
+        const double L2 = L * L, f = (T - 24.5) * (T + 570.82), df = 2.0 * T + 546.32;
+        const double c3 = a3 + b3 * f, den1 = L2 - c3 * c3, den2 = L2 - a5 * a5;
+        const double n2 = a1 + b1 * f + (a2 + b2 * f) / den1 + (a4 + b4 * f) / den2 - a6 * L2;
+        const double dn2 = (b1 + b2 / den1 + (a2 + b2 * f) * 2.0 * c3 * b3 / (den1 * den1) + b4 / den2) * df;
+        return dn2 / (2 * std::sqrt(n2));
+    }
+    return sellmeier_dT(L, T);
+}
+
 // dn/dT of Crystal.h:116-132 in double (the smooth model behind the float index).
 double sellmeier_dT(double L, double T) {
     const double A = 4.502483, B = 0.007294, C = 0.185087, D = -0.02357, E = 0.073423, F = 0.199595, G = 0.001,
@@ -189,7 +204,7 @@ int adjoint_run(const shg_config &cfg, const InstDesc &h, const InstDesc *d, flo
     if (rc) return rc;
     // loss scale: P_SH = 1/2 eps0 c n_s dx dy sum |S_out|^2; the seed is 2 * that scale
     const float lp = cfg.lp, ls = (float)(0.5 * (double)lp);
-    const float ns = sellmeier(ls, temp), np = sellmeier(lp, temp);
+    const float ns = crystal_index(cfg.crystal, ls, temp), np = crystal_index(cfg.crystal, lp, temp);
     const double kl = field_power(1.0, ns, h.dx, h.dy);
     const double seed = 2.0 * kl;
     AD_CUDA(cudaMemcpyAsync(w.acc_glob + 3, &seed, sizeof(double), cudaMemcpyHostToDevice, st));
@@ -245,7 +260,7 @@ int adjoint_run(const shg_config &cfg, const InstDesc &h, const InstDesc *d, flo
     const double ksw = 2.0 * 3.14159265358979323846 * (double)ns / (double)ls;
     const double dL_dkpw = g[0] * (double)h.dz * (double)h.gp / kpw;
     const double dL_dksw = g[1] * (double)h.dz * (double)h.gs / ksw;
-    const double dnp = sellmeier_dT(lp, temp), dns = sellmeier_dT(ls, temp);
+    const double dnp = crystal_index_dT(cfg.crystal, lp, temp), dns = crystal_index_dT(cfg.crystal, ls, temp);
     const double two_pi = 2.0 * 3.14159265358979323846;
     const double ddk_dT = two_pi * (2.0 * dnp / lp - dns / ls);
     const double dT = dL_ddk * ddk_dT + dL_dkp * (-(double)h.kp / np) * dnp + dL_dks * (-(double)h.ks / ns) * dns +
@@ -264,7 +279,7 @@ int pump_param_gradients(const shg_config &cfg, const InstDesc &h, float power, 
     // Efields.h:74-104 constants in double from the float index the reference uses
     const double PI = 3.14159265358979323846;
     const double eps0 = (double)(float)(8.8541878128E-12 * 1E12 / 1E6), c = (double)(float)(299792458 * 1E6 / 1E12);
-    const double np = (double)sellmeier(cfg.lp, temp);
+    const double np = (double)crystal_index(cfg.crystal, cfg.lp, temp);
     const double w_ = waist, w2 = w_ * w_;
     const double zr = PI * np * w2 / (double)cfg.lp;
     const double ap0 = std::sqrt(4.0 * (double)power / (eps0 * c * PI * np * w2));
@@ -277,7 +292,7 @@ int pump_param_gradients(const shg_config &cfg, const InstDesc &h, float power, 
     out4[0] = r[0];
     out4[1] = r[1];
     out4[2] = r[2];
-    out4[3] = r[3] * sellmeier_dT(cfg.lp, temp);
+    out4[3] = r[3] * crystal_index_dT(cfg.crystal, cfg.lp, temp);
     return SHG_OK;
 }
 

@@ -122,7 +122,7 @@ int ThermalGradBatch::setup_solve(int i, float power, float waist, float focal) 
     // Efields.h:74-126: Gaussian pump and shifted propagators at the centre temperature
     TG_CUDA(launch_setup(d_desc_ + i, 1, (int)nn_, nz_, st));
     // loss scale: P_SH = 1/2 eps0 c n_s(tc) dx dy sum |S|^2 (the efficiency's convention)
-    const float ns = sellmeier((float)(0.5 * (double)cfg_.lp), tc);
+    const float ns = crystal_index(cfg_.crystal, (float)(0.5 * (double)cfg_.lp), tc);
     const double seed = 2.0 * field_power(1.0, ns, h.dx, h.dy);
     TG_CUDA(cudaMemcpyAsync(seed_ + i, &seed, sizeof(double), cudaMemcpyHostToDevice, st));
     TG_CUDA(cudaStreamSynchronize(st));
@@ -281,7 +281,8 @@ int ThermalGradBatch::finish(double *p_sh, double *p_in, cudaStream_t st) {
     TG_CUDA(cudaMemcpyAsync(s.data(), sums_, s.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
     TG_CUDA(cudaStreamSynchronize(st));
     for (int b = 0; b < count_; ++b) {
-        const float np = sellmeier(cfg_.lp, tc_[b]), ns = sellmeier((float)(0.5 * (double)cfg_.lp), tc_[b]);
+        const float np = crystal_index(cfg_.crystal, cfg_.lp, tc_[b]),
+                    ns = crystal_index(cfg_.crystal, (float)(0.5 * (double)cfg_.lp), tc_[b]);
         if (p_sh) p_sh[b] = field_power(s[b], ns, h_desc_[b].dx, h_desc_[b].dy);
         if (p_in) p_in[b] = field_power(s[count_ + b], np, h_desc_[b].dx, h_desc_[b].dy);
     }

@@ -73,6 +73,28 @@ float sellmeier(float L, float T) {
     return (float)std::sqrt(n2);
 }
 
+// Extraordinary index of periodically poled lithium niobate (congruent LiNbO3): the
+// temperature-dependent Sellmeier fit of D. H. Jundt, Opt. Lett. 22, 1553-1555 (1997),
+// L in um, T in C:
+//   n^2 = a1 + b1 f + (a2 + b2 f) / (L^2 - (a3 + b3 f)^2) + (a4 + b4 f) / (L^2 - a5^2) - a6 L^2,
+//   f = (T - 24.5) (T + 570.82).
+// Evaluated in double and rounded to float, like the reference's sPPLT routine. The
+// reference's code holds no LiNbO3 routine (its README names an MgO:PPLN crystal), so
+// nothing in the reference pins these values; they are the published fit.
+float sellmeier_ln(float L, float T) {
+    const double a1 = 5.35583, a2 = 0.100473, a3 = 0.20692, a4 = 100.0, a5 = 11.34927, a6 = 1.5334e-2;
+    const double b1 = 4.629e-7, b2 = 3.862e-8, b3 = -0.89e-8, b4 = 2.657e-5;
+    const double t = (double)T, L2 = (double)L * (double)L;
+    const double f = (t - 24.5) * (t + 570.82);
+    const double c3 = a3 + b3 * f;
+    const double n2 = a1 + b1 * f + (a2 + b2 * f) / (L2 - c3 * c3) + (a4 + b4 * f) / (L2 - a5 * a5) - a6 * L2;
+    return (float)std::sqrt(n2);
+}
+
+float crystal_index(int crystal, float L, float T) {
+    return crystal == SHG_CRYSTAL_PPLN ? sellmeier_ln(L, T) : sellmeier(L, T);
+}
+
 // Fill the scalar part of a descriptor (pointers are set by the caller).
 void fill_scalars(const shg_config &cr, const SolveParams &sp, InstDesc &d) {
     const Phys ph;
@@ -89,7 +111,7 @@ void fill_scalars(const shg_config &cr, const SolveParams &sp, InstDesc &d) {
     d.dz = dz;
     d.dz6 = dz / 6.0f;
     // Solver.h:75-77: i*pi*dQ/(n_p*lp), i*0.5*pi*dQ/(n_s*ls); TPA and absorption terms.
-    const float np_t = sellmeier(lp, sp.temp), ns_t = sellmeier(ls, sp.temp);
+    const float np_t = crystal_index(cr.crystal, lp, sp.temp), ns_t = crystal_index(cr.crystal, ls, sp.temp);
     d.kp = (dQ * PI) / (np_t * lp);
     d.ks = (dQ * (PI * 0.5f)) / (ns_t * ls);
     d.hp = (float)(0.5 * (double)cr.alpha_p);
@@ -98,7 +120,7 @@ void fill_scalars(const shg_config &cr, const SolveParams &sp, InstDesc &d) {
     // PhaseMatching.h:57-70
     d.dk = 2.0f * PI * (2.0f * np_t / lp - ns_t / ls + 1.0f / cr.lambda_qpm);
     // Efields.h:74-104 at tpump
-    const float np_c = sellmeier(lp, sp.tpump);
+    const float np_c = crystal_index(cr.crystal, lp, sp.tpump);
     d.uX = (float)(0.5 * n);
     d.uY = (float)(0.5 * n);
     d.dx = dx;
@@ -113,7 +135,7 @@ void fill_scalars(const shg_config &cr, const SolveParams &sp, InstDesc &d) {
     d.wM = make_float2(wX2 * mre, wX2 * mim);
     d.wM_den = d.wM.x * d.wM.x + d.wM.y * d.wM.y;
     // Efields.h:107-126 at tprop
-    const float np_h = sellmeier(lp, sp.tprop), ns_h = sellmeier(ls, sp.tprop);
+    const float np_h = crystal_index(cr.crystal, lp, sp.tprop), ns_h = crystal_index(cr.crystal, ls, sp.tprop);
     const float kpw = 2.0f * PI * np_h / lp, ksw = 2.0f * PI * ns_h / ls;
     const float dfX = 1.0f / dx / (float)(unsigned)n, dfY = 1.0f / dy / (float)(unsigned)n;
     const float pi2 = PI * PI;
@@ -732,7 +754,8 @@ class Batch {
     double eta_of(int i, const std::vector<double> &acc) const {
         const SolveParams &s = sp_[i];
         const float dx = desc_[i].dx, dy = desc_[i].dy;
-        const float np_c = sellmeier(cr_.lp, s.temp), ns_c = sellmeier((float)(0.5 * (double)cr_.lp), s.temp);
+        const float np_c = crystal_index(cr_.crystal, cr_.lp, s.temp),
+                    ns_c = crystal_index(cr_.crystal, (float)(0.5 * (double)cr_.lp), s.temp);
         const double pin = field_power(acc[4 * i + 0], np_c, dx, dy);
         const double psh = field_power(acc[4 * i + 1], ns_c, dx, dy);
         return psh / pin;
@@ -741,7 +764,8 @@ class Batch {
     void powers_of(int i, const std::vector<double> &acc, double *pin, double *psh, double *pout) const {
         const SolveParams &s = sp_[i];
         const float dx = desc_[i].dx, dy = desc_[i].dy;
-        const float np_c = sellmeier(cr_.lp, s.temp), ns_c = sellmeier((float)(0.5 * (double)cr_.lp), s.temp);
+        const float np_c = crystal_index(cr_.crystal, cr_.lp, s.temp),
+                    ns_c = crystal_index(cr_.crystal, (float)(0.5 * (double)cr_.lp), s.temp);
         if (pin) *pin = field_power(acc[4 * i + 0], np_c, dx, dy);
         if (psh) *psh = field_power(acc[4 * i + 1], ns_c, dx, dy);
         if (pout) *pout = field_power(acc[4 * i + 2], np_c, dx, dy);
@@ -970,6 +994,10 @@ class Batch {
 };
 
 int validate_config(const shg_config &c) {
+    if (c.crystal != SHG_CRYSTAL_SPPLT && c.crystal != SHG_CRYSTAL_PPLN) {
+        set_error("crystal must be SHG_CRYSTAL_SPPLT or SHG_CRYSTAL_PPLN");
+        return SHG_ERR_INVALID;
+    }
     if (c.nx <= 1 || c.ny <= 1 || c.nz <= 1) {
         set_error("grid sizes must be > 1");
         return SHG_ERR_INVALID;
@@ -1125,6 +1153,20 @@ int shg_config_init(shg_config *c) {
     c->bc = 0;
     c->sh_seed = -1;
     c->device = 0;
+    c->crystal = SHG_CRYSTAL_SPPLT;
+    return SHG_OK;
+}
+
+int shg_index(int crystal, float lambda_um, float temp_c, float *n) {
+    if (!n || (crystal != SHG_CRYSTAL_SPPLT && crystal != SHG_CRYSTAL_PPLN) || !(lambda_um > 0)) {
+        set_error("shg_index: unknown crystal, non-positive wavelength or null output");
+        return SHG_ERR_INVALID;
+    }
+    *n = crystal_index(crystal, lambda_um, temp_c);
+    if (!std::isfinite(*n)) {
+        set_error("shg_index: the index is not finite at this wavelength and temperature");
+        return SHG_ERR_NONFINITE;
+    }
     return SHG_OK;
 }
 
@@ -1484,6 +1526,10 @@ int shg_get_jacobi_counts(shg_handle *h, int *counts) {
 int shg_batch_create(const shg_config *crystal, const shg_instance *inst, int n, shg_batch **out) {
     if (!crystal || !inst || !out || n <= 0) {
         set_error("null argument or empty batch");
+        return SHG_ERR_INVALID;
+    }
+    if (crystal->crystal != SHG_CRYSTAL_SPPLT && crystal->crystal != SHG_CRYSTAL_PPLN) {
+        set_error("crystal must be SHG_CRYSTAL_SPPLT or SHG_CRYSTAL_PPLN");
         return SHG_ERR_INVALID;
     }
     *out = nullptr;

@@ -65,8 +65,9 @@ cudaError_t heat_error_word_acquire(int **err);
 void heat_error_word_release(int *err);
 cudaError_t launch_sq_diff_sum(const float *Tf, const float *Ti, size_t n, double *out, cudaStream_t st);
 cudaError_t launch_sq_sums(const float *Tf, const float *Ti, size_t n, double *out2, cudaStream_t st);
+// crystal: SHG_CRYSTAL_SPPLT (Crystal.h:55-71) or SHG_CRYSTAL_PPLN (sellmeier_ln).
 cudaError_t launch_sellmeier_tables(const float *T, float *NP, float *NS, float *DK, size_t n, float lp, float ls,
-                                    float two_pi, float inv_lambda, cudaStream_t st);
+                                    float two_pi, float inv_lambda, int crystal, cudaStream_t st);
 cudaError_t launch_rows_th(int n, const InstDesc *d, const ThermDesc &th, int s, cudaStream_t st);
 
 // One solve's run parameters (Solver::run arguments and the temperatures its set-up
@@ -86,7 +87,9 @@ bool save_tensor_real(const std::string &dir, const std::string &name, const flo
 
 // shg_host.cpp
 void set_error(const std::string &msg);
-float sellmeier(float L, float T);
+float sellmeier(float L, float T);     // Crystal.h:55-71 (MgO:sPPLT)
+float sellmeier_ln(float L, float T);  // PPLN (congruent LiNbO3, Jundt 1997)
+float crystal_index(int crystal, float L, float T);
 void fill_scalars(const shg_config &cr, const SolveParams &sp, InstDesc &d);
 double field_power(double sum_abs2, float n_index, float dx, float dy);
 int ensure_twiddles(int device);

@@ -115,6 +115,10 @@ extern "C" int shg_cwes_noalloc(const shg_config *cfg, float temp, const void *p
         set_error("shg_cwes_noalloc: NZ must be in [2, " + std::to_string(kNoAllocMaxNz) + "] (fixed scratch size)");
         return SHG_ERR_INVALID;
     }
+    if (cfg->crystal != SHG_CRYSTAL_SPPLT && cfg->crystal != SHG_CRYSTAL_PPLN) {
+        set_error("shg_cwes_noalloc: unknown crystal");
+        return SHG_ERR_INVALID;
+    }
     if (!(cfg->lx > 0) || !(cfg->ly > 0) || !(cfg->lz > 0)) {
         set_error("shg_cwes_noalloc: window and crystal length must be positive");
         return SHG_ERR_INVALID;
@@ -162,7 +166,8 @@ extern "C" int shg_cwes_noalloc(const shg_config *cfg, float temp, const void *p
         double acc[4] = {0, 0, 0, 0};
         NOALLOC_CUDA(cudaMemcpyAsync(acc, d.acc, sizeof(acc), cudaMemcpyDeviceToHost, st));
         NOALLOC_CUDA(cudaStreamSynchronize(st));
-        const float np_t = sellmeier(cfg->lp, temp), ns_t = sellmeier((float)(0.5 * (double)cfg->lp), temp);
+        const float np_t = crystal_index(cfg->crystal, cfg->lp, temp),
+                    ns_t = crystal_index(cfg->crystal, (float)(0.5 * (double)cfg->lp), temp);
         *eta = field_power(acc[1], ns_t, d.dx, d.dy) / field_power(acc[0], np_t, d.dx, d.dy);
     }
     return SHG_OK;

@@ -449,12 +449,29 @@ __device__ __forceinline__ float sellmeier_dev(float L, float T) {
     return __double2float_rn(__dsqrt_rn(n2));
 }
 
+// PPLN index (the congruent LiNbO3 fit of sellmeier_ln, shg_host.cpp) in double with no
+// contraction: bit-identical to the host evaluation.
+__device__ __forceinline__ float sellmeier_ln_dev(float L, float T) {
+    const double a1 = 5.35583, a2 = 0.100473, a3 = 0.20692, a4 = 100.0, a5 = 11.34927, a6 = 1.5334e-2;
+    const double b1 = 4.629e-7, b2 = 3.862e-8, b3 = -0.89e-8, b4 = 2.657e-5;
+    const double t = (double)T, L2 = __dmul_rn((double)L, (double)L);
+    const double f = __dmul_rn(__dsub_rn(t, 24.5), __dadd_rn(t, 570.82));
+    const double c3 = __dadd_rn(a3, __dmul_rn(b3, f));
+    double n2 = __dadd_rn(a1, __dmul_rn(b1, f));
+    n2 = __dadd_rn(n2, __ddiv_rn(__dadd_rn(a2, __dmul_rn(b2, f)), __dsub_rn(L2, __dmul_rn(c3, c3))));
+    n2 = __dadd_rn(n2, __ddiv_rn(__dadd_rn(a4, __dmul_rn(b4, f)), __dsub_rn(L2, __dmul_rn(a5, a5))));
+    n2 = __dsub_rn(n2, __dmul_rn(a6, L2));
+    return __double2float_rn(__dsqrt_rn(n2));
+}
+
 // PhaseMatching.h:41-54 per voxel, plus the two indices the thermal z-march needs.
+template <int CRYSTAL>
 __global__ void k_sellmeier_tables(const float *__restrict__ T, float *NP, float *NS, float *DK, size_t n, float lp,
                                    float ls, float two_pi, float inv_lambda) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         const float t = T[i];
-        const float np = sellmeier_dev(lp, t), ns = sellmeier_dev(ls, t);
+        const float np = CRYSTAL == 1 ? sellmeier_ln_dev(lp, t) : sellmeier_dev(lp, t);
+        const float ns = CRYSTAL == 1 ? sellmeier_ln_dev(ls, t) : sellmeier_dev(ls, t);
         NP[i] = np;
         NS[i] = ns;
         DK[i] = __fmul_rn(two_pi, __fadd_rn(__fsub_rn(__fdiv_rn(__fmul_rn(2.0f, np), lp), __fdiv_rn(ns, ls)), inv_lambda));
@@ -722,8 +739,11 @@ cudaError_t launch_sq_diff_sum(const float *Tf, const float *Ti, size_t n, doubl
 }
 
 cudaError_t launch_sellmeier_tables(const float *T, float *NP, float *NS, float *DK, size_t n, float lp, float ls,
-                                    float two_pi, float inv_lambda, cudaStream_t st) {
-    k_sellmeier_tables<<<2432, 256, 0, st>>>(T, NP, NS, DK, n, lp, ls, two_pi, inv_lambda);
+                                    float two_pi, float inv_lambda, int crystal, cudaStream_t st) {
+    if (crystal == 1)
+        k_sellmeier_tables<1><<<2432, 256, 0, st>>>(T, NP, NS, DK, n, lp, ls, two_pi, inv_lambda);
+    else
+        k_sellmeier_tables<0><<<2432, 256, 0, st>>>(T, NP, NS, DK, n, lp, ls, two_pi, inv_lambda);
     return cudaGetLastError();
 }
 

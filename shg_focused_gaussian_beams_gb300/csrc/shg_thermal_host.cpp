@@ -256,7 +256,8 @@ int ThermalSolve::tables() {
     const float PI = (float)3.14159265358979323846;
     const float lp = cfg_.lp, ls = (float)(0.5 * (double)lp);
     // PhaseMatching.h:105 -> 41: delta-k and the indices from T.
-    TH_CUDA(launch_sellmeier_tables(T_cur(), np_, ns_, dk_, tsize_, lp, ls, 2 * PI, 1 / (cfg_.lambda_qpm), st_));
+    TH_CUDA(launch_sellmeier_tables(T_cur(), np_, ns_, dk_, tsize_, lp, ls, 2 * PI, 1 / (cfg_.lambda_qpm), cfg_.crystal,
+                                    st_));
     // Efields.h:77,110: pump and propagators use T at the grid centre of slice 0.
     const size_t ic = (size_t)(n_ / 2) * n_ + (size_t)(n_ / 2);
     TH_CUDA(cudaMemcpyAsync(&tc_, T_cur() + ic, sizeof(float), cudaMemcpyDeviceToHost, st_));
@@ -379,7 +380,8 @@ int ThermalSolve::powers(double *pin, double *psh, double *pout) {
     double acc[4];
     TH_CUDA(cudaStreamSynchronize(st_));
     TH_CUDA(cudaMemcpy(acc, acc_, sizeof(acc), cudaMemcpyDeviceToHost));
-    const float np_c = sellmeier(cfg_.lp, tc_), ns_c = sellmeier((float)(0.5 * (double)cfg_.lp), tc_);
+    const float np_c = crystal_index(cfg_.crystal, cfg_.lp, tc_),
+                ns_c = crystal_index(cfg_.crystal, (float)(0.5 * (double)cfg_.lp), tc_);
     const float dx = cfg_.lx / (float)(unsigned)(n_ - 1), dy = cfg_.ly / (float)(unsigned)(n_ - 1);
     if (pin) *pin = field_power(acc[0], np_c, dx, dy);
     if (psh) *psh = field_power(acc[1], ns_c, dx, dy);
@@ -405,6 +407,10 @@ int thermal_component_cfg(const shg_config *cfg) {
     if (cfg->nx != cfg->ny) {
         set_error("the device thermal path needs NX = NY");
         return SHG_ERR_UNSUPPORTED;
+    }
+    if (cfg->crystal != SHG_CRYSTAL_SPPLT && cfg->crystal != SHG_CRYSTAL_PPLN) {
+        set_error("crystal must be SHG_CRYSTAL_SPPLT or SHG_CRYSTAL_PPLN");
+        return SHG_ERR_INVALID;
     }
     return SHG_OK;
 }
@@ -488,7 +494,7 @@ int shg_dk_thermal(const shg_config *cfg, const float *T, float *DK, float *NP, 
     const float lp = cfg->lp, ls = (float)(0.5 * (double)lp);
     cudaError_t e = cudaMemcpy(ts.T_cur(), T, n * sizeof(float), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = launch_sellmeier_tables(ts.T_cur(), d, d + n, d + 2 * n, n, lp, ls, 2 * PI,
-                                                      1 / (cfg->lambda_qpm), ts.stream());
+                                                      1 / (cfg->lambda_qpm), cfg->crystal, ts.stream());
     if (e == cudaSuccess) e = cudaStreamSynchronize(ts.stream());
     if (e == cudaSuccess) e = cudaMemcpy(tmp.data(), d, 3 * n * sizeof(float), cudaMemcpyDeviceToHost);
     cudaFree(d);

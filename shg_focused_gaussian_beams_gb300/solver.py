@@ -25,6 +25,8 @@ def _cfg_from(crystal=None, **kw) -> _lib.Config:
                   "rho_s", "kth", "htc"):
             if k in src:
                 setattr(cfg, k, float(src[k]))
+        if "crystal" in src:
+            cfg.crystal = int(src["crystal"])
     for k, v in kw.items():
         setattr(cfg, k, v)
     return cfg

@@ -10,7 +10,11 @@ Units follow the reference (Crystal.h:19-21): micrometres, picoseconds, volts, w
 
 ``sellmeier_n`` reproduces the reference's Sellmeier routine bit for bit (float
 arguments, double evaluation, float result; Crystal.h:116-132), which the workload
-definitions need to place the poling period and the pump waist.
+definitions need to place the poling period and the pump waist. ``crystal=1`` selects
+periodically poled lithium niobate with the congruent-LiNbO3 Sellmeier fit of Jundt,
+Opt. Lett. 22, 1553 (1997) (``ln_n``; the reference's README names an MgO:PPLN crystal,
+whose index its code does not hold); ``CRYSTAL_PPLN_QPM50`` is the plain workload's
+crystal with that index and its own poling period for phase matching at 50 C.
 """
 from __future__ import annotations
 
@@ -43,17 +47,35 @@ def sellmeier_n(L: float, T: float) -> np.float32:
     return F32(math.sqrt(n2))
 
 
-def qpm_period(T: float, lp: float = LP_UM) -> float:
+def ln_n(L: float, T: float) -> np.float32:
+    """Extraordinary index of congruent LiNbO3 (PPLN; Jundt, Opt. Lett. 22, 1553-1555
+    (1997)): n^2 = a1 + b1 f + (a2 + b2 f)/(L^2 - (a3 + b3 f)^2) + (a4 + b4 f)/(L^2 - a5^2)
+    - a6 L^2 with f = (T - 24.5)(T + 570.82); double, rounded to float."""
+    a1, a2, a3, a4, a5, a6 = 5.35583, 0.100473, 0.20692, 100.0, 11.34927, 1.5334e-2
+    b1, b2, b3, b4 = 4.629e-7, 3.862e-8, -0.89e-8, 2.657e-5
+    t, L2 = float(F32(T)), float(F32(L)) ** 2
+    f = (t - 24.5) * (t + 570.82)
+    c3 = a3 + b3 * f
+    n2 = a1 + b1 * f + (a2 + b2 * f) / (L2 - c3 * c3) + (a4 + b4 * f) / (L2 - a5 * a5) - a6 * L2
+    return F32(math.sqrt(n2))
+
+
+def index_n(L: float, T: float, crystal: int = 0) -> np.float32:
+    """n(L, T) of the selected crystal: 0 MgO:sPPLT (the reference's), 1 PPLN."""
+    return ln_n(L, T) if crystal == 1 else sellmeier_n(L, T)
+
+
+def qpm_period(T: float, lp: float = LP_UM, crystal: int = 0) -> float:
     """Poling period that phase-matches 2*k_p = k_s at oven temperature T, rounded to
     float: Lambda = lp / (2 (n_s - n_p))."""
-    n_p = float(sellmeier_n(lp, T))
-    n_s = float(sellmeier_n(F32(0.5 * lp), T))
+    n_p = float(index_n(lp, T, crystal))
+    n_s = float(index_n(F32(0.5 * lp), T, crystal))
     return float(F32(lp / (2.0 * (n_s - n_p))))
 
 
-def waist_for_xi(xi: float, T: float, lz: float = LZ_UM, lp: float = LP_UM) -> float:
+def waist_for_xi(xi: float, T: float, lz: float = LZ_UM, lp: float = LP_UM, crystal: int = 0) -> float:
     """Pump waist radius giving focusing parameter xi = L / (2 z_R), z_R = pi n_p w0^2 / lp."""
-    n_p = float(sellmeier_n(lp, T))
+    n_p = float(index_n(lp, T, crystal))
     zr = lz / (2.0 * xi)
     return float(F32(math.sqrt(zr * lp / (math.pi * n_p))))
 
@@ -74,12 +96,15 @@ class Crystal:
     rho_s: float = 0.0
     kth: float = 8.4e-6
     htc: float = 10e-12
+    crystal: int = 0                 # refractive index: 0 MgO:sPPLT (Crystal.h), 1 PPLN (LiNbO3)
 
 
 CRYSTAL_REFERENCE = Crystal(name="MgO:sPPLT (reference defaults)")
 PM_TEMP_C = 50.0
 CRYSTAL_QPM50 = Crystal(name="MgO:sPPLT QPM@50C", deff=6.75e-6, lambda_qpm=qpm_period(PM_TEMP_C),
                         alpha_p=2e-7, alpha_s=4e-6, beta_s=1e-5)
+CRYSTAL_PPLN_QPM50 = Crystal(name="PPLN QPM@50C", deff=6.75e-6, lambda_qpm=qpm_period(PM_TEMP_C, crystal=1),
+                             alpha_p=2e-7, alpha_s=4e-6, beta_s=1e-5, crystal=1)
 
 
 @dataclass
