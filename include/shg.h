@@ -195,15 +195,20 @@ int shg_batch_launch_count(shg_batch *b, int *launches);
  * solve, fields in shared memory) in one of several (cluster size, CTAs per SM) variants.
  * Resident variants also differ in the line-FFT split (n = 64: 8 x 8 or 16 x 4 points).
  * Unless the environment variable SHG_MARCH is "streaming", "resident" (default variants)
- * or lists a schedule per grid ("64:1/1,128:4/2,256:16/2", "64:1/1/4", "64:streaming"), the first run
- * times every candidate on the class's own solves and keeps the fastest (cached per
- * device and class shape for the process). shg_batch_autotune does that now, outside any
+ * or lists a schedule per grid ("64:1/1,128:4/2,256:16/2", "64:1/1/4", "64:streaming",
+ * "128:coop"), the first run times every candidate on the class's own solves and keeps the
+ * fastest (cached per device and class shape for the process). A batch of one solve has one
+ * more candidate, "coop": the whole march in one cooperative launch (row and column passes
+ * of the streaming kernels, bit-identical, separated by grid-wide barriers whose waits are
+ * bounded; a wait that gives up makes the run's result calls return SHG_ERR_CUDA). shg_batch_autotune does that now, outside any
  * stream capture; shg_batch_schedule writes the choices and trial times as text. */
 int shg_batch_autotune(shg_batch *b, void *stream);
-/* Fixes the schedule of the class with grid n: resident = 0 streaming, else the resident
- * variant with cluster_size CTAs per cluster and ctas_per_sm CTAs per SM (variants: n <= 32
- * (1, 1); n = 64 (1, 1), (1, 2), (2, 2), (2, 4); n = 128 (2, 1), (4, 1), (4, 2); n = 256
- * (8, 1), (16, 1), (16, 2)). SHG_ERR_UNSUPPORTED if the variant does not exist or fit. */
+/* Fixes the schedule of the class with grid n: resident = 0 streaming, resident = 2 the
+ * persistent cooperative grid (a batch of one solve only; cluster_size and ctas_per_sm
+ * unused), else the resident variant with cluster_size CTAs per cluster and ctas_per_sm
+ * CTAs per SM (variants: n <= 32 (1, 1); n = 64 (1, 1), (1, 2), (2, 2), (2, 4); n = 128
+ * (2, 1), (4, 1), (4, 2); n = 256 (8, 1), (16, 1), (16, 2)). SHG_ERR_UNSUPPORTED if the
+ * variant does not exist or fit. */
 int shg_batch_set_schedule(shg_batch *b, int n, int resident, int cluster_size, int ctas_per_sm);
 /* Same for a resident variant with a given line-FFT split: threads_per_line G, each thread
  * holding N/G points (n = 64: G = 8 or 4; other grids: their one split). */

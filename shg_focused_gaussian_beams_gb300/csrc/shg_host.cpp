@@ -194,6 +194,13 @@ int ensure_twiddles(int device) {
     return SHG_OK;
 }
 
+// Name of a class schedule: "streaming", "coop" (persistent grid) or "cs/minb/g".
+std::string schedule_label(bool resident, const ResidentVariant &v) {
+    if (!resident) return "streaming";
+    if (v.cs == 0) return "coop";
+    return std::to_string(v.cs) + "/" + std::to_string(v.minb) + "/" + std::to_string(v.g);
+}
+
 // ---------------------------------------------------------------------------------------
 // A set of plain solves with their device buffers and launch schedule.
 class Batch {
@@ -295,7 +302,8 @@ class Batch {
         }
         // schedule per class from SHG_MARCH: "auto" (default: the autotuner picks at the first
         // run), "streaming", "resident" (default variants), or a list "n:streaming" /
-        // "n:cs/minb" per grid (e.g. "64:1/1,128:4/2,256:16/2"; unlisted grids: autotuner)
+        // "n:cs/minb" / "n:coop" per grid (e.g. "64:1/1,128:4/2,256:16/2"; unlisted grids:
+        // autotuner; "coop", the persistent cooperative grid, applies to a batch of one solve)
         const char *mode = std::getenv("SHG_MARCH");
         const std::string m = mode ? mode : "auto";
         for (auto &c : classes_) {
@@ -315,6 +323,12 @@ class Batch {
                 if (v == "streaming") {
                     c.resident = false;
                     c.tuned = true;
+                } else if (v == "coop") {
+                    if (classes_.size() == 1 && c.count == 1) {
+                        c.resident = true;
+                        c.var = ResidentVariant{0, 0, 0};
+                        c.tuned = true;
+                    }
                 } else if (std::sscanf(v.c_str(), "%d/%d/%d", &cs, &mb, &g) >= 2) {
                     ResidentVariant vs[16];
                     const int nv = resident_variants(c.n, vs, 16);
@@ -434,6 +448,10 @@ class Batch {
         return SHG_OK;
     }
 
+    // The persistent cooperative grid is offered only to a batch of one solve: it holds every
+    // SM it is given, so it never shares the device with another class's side stream.
+    bool lone_solve() const { return classes_.size() == 1 && classes_[0].count == 1; }
+
     int launch_count() const {
         int c = 2;  // set-up kernels
         for (const auto &k : classes_) {
@@ -456,7 +474,7 @@ class Batch {
             desc_dirty_ = false;
         }
         static std::mutex mu;
-        static std::map<std::tuple<int, int, int, double>, std::pair<bool, ResidentVariant>> cache;
+        static std::map<std::tuple<int, int, int, double, bool>, std::pair<bool, ResidentVariant>> cache;
         cudaEvent_t a, b;
         SHG_CUDA(cudaEventCreate(&a));
         SHG_CUDA(cudaEventCreate(&b));
@@ -464,7 +482,7 @@ class Batch {
         for (int ci = 0; ci < (int)classes_.size() && rc == SHG_OK; ++ci) {
             Class &c = classes_[ci];
             if (c.tuned) continue;
-            const auto key = std::make_tuple(cr_.device, c.n, c.count, c.pt_steps);
+            const auto key = std::make_tuple(cr_.device, c.n, c.count, c.pt_steps, lone_solve());
             {
                 std::lock_guard<std::mutex> lock(mu);
                 auto it = cache.find(key);
@@ -490,6 +508,13 @@ class Batch {
                     cands.push_back({true, vs[i], mc});
                 else
                     cudaGetLastError();  // a variant that does not fit is skipped
+            }
+            if (lone_solve()) {  // one solve in the batch: the persistent cooperative grid as well
+                int mc = 0;
+                if (prepare_resident(c.n, ResidentVariant{0, 0, 0}, &mc) == cudaSuccess && mc > 0)
+                    cands.push_back({true, ResidentVariant{0, 0, 0}, 1});
+                else
+                    cudaGetLastError();
             }
             float best = 1e30f;
             int bi = 0;
@@ -608,10 +633,7 @@ class Batch {
                 r /= (int)opts[oi].size();
                 const Pick &p = opts[oi][k];
                 SHG_TRY_INT(apply(order[oi], p));
-                label += (oi ? "," : "") + std::to_string(classes_[order[oi]].n) + ":" +
-                         (p.resident ? std::to_string(p.v.cs) + "/" + std::to_string(p.v.minb) + "/" +
-                                           std::to_string(p.v.g)
-                                     : std::string("streaming"));
+                label += (oi ? "," : "") + std::to_string(classes_[order[oi]].n) + ":" + schedule_label(p.resident, p.v);
             }
             // time the combination as runs execute it: a captured graph, second launch counted
             float ms = 0.f;
@@ -648,6 +670,16 @@ class Batch {
             if (c.n != n) continue;
             if (!resident) {
                 c.resident = false;
+            } else if (resident == 2) {
+                int mc = 0;
+                if (!lone_solve() || prepare_resident(n, ResidentVariant{0, 0, 0}, &mc) != cudaSuccess || mc < 1) {
+                    cudaGetLastError();
+                    set_error("set_schedule: the persistent grid runs a batch of one solve whose grid fits co-resident");
+                    return SHG_ERR_UNSUPPORTED;
+                }
+                c.resident = true;
+                c.var = ResidentVariant{0, 0, 0};
+                c.max_clusters = 1;
             } else {
                 ResidentVariant vs[16];
                 const int nv = resident_variants(n, vs, 16);
@@ -712,19 +744,17 @@ class Batch {
         std::string out;
         for (const auto &c : classes_) {
             out += "n=" + std::to_string(c.n) + " solves=" + std::to_string(c.count) + ": ";
-            out += !c.tuned ? "untuned" : c.resident ? "resident cs=" + std::to_string(c.var.cs) +
-                                                             " minb=" + std::to_string(c.var.minb) +
-                                                             " g=" + std::to_string(c.var.g)
-                                                       : std::string("streaming");
+            out += !c.tuned                      ? std::string("untuned")
+                   : !c.resident                   ? std::string("streaming")
+                   : c.var.cs == 0                 ? std::string("coop (persistent grid)")
+                                                   : "resident cs=" + std::to_string(c.var.cs) + " minb=" +
+                                                       std::to_string(c.var.minb) + " g=" + std::to_string(c.var.g);
             if (!c.trials.empty()) {
                 out += " [";
                 for (size_t i = 0; i < c.trials.size(); ++i) {
                     const auto &t = c.trials[i];
                     char buf[96];
-                    std::snprintf(buf, sizeof(buf), "%s%s %.3f", i ? ", " : "",
-                                  t.resident ? ("cs" + std::to_string(t.v.cs) + "/" + std::to_string(t.v.minb) + "/" +
-                                                std::to_string(t.v.g)).c_str()
-                                             : "streaming",
+                    std::snprintf(buf, sizeof(buf), "%s%s %.3f", i ? ", " : "", schedule_label(t.resident, t.v).c_str(),
                                   t.ms);
                     out += buf;
                 }
@@ -747,6 +777,18 @@ class Batch {
     int copy_acc(std::vector<double> &acc) {
         acc.resize(4 * desc_.size());
         SHG_CUDA(cudaMemcpy(acc.data(), acc_, acc.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        return check_run_errors();
+    }
+
+    // Error word of the last run (set when a grid-barrier wait of the persistent grid gave up);
+    // read after the run has completed.
+    int check_run_errors() {
+        int flag = 0;
+        SHG_CUDA(cudaMemcpy(&flag, d_counters_ + 63, sizeof(int), cudaMemcpyDeviceToHost));
+        if (flag) {
+            set_error("persistent grid: a grid-barrier wait gave up (run incomplete)");
+            return SHG_ERR_CUDA;
+        }
         return SHG_OK;
     }
 
@@ -909,6 +951,14 @@ class Batch {
     int enqueue_class(int ci, cudaStream_t st, Recorder *rec) {
         const Class &k = classes_[ci];
         const int *list = d_lists_ + k.offset;
+        if (k.resident && k.var.cs == 0) {
+            // the persistent cooperative grid of a lone solve: barrier words 40 + 2 ci, error word 63
+            unsigned *bar = reinterpret_cast<unsigned *>(d_counters_ + 40 + 2 * ci);
+            if (rec) SHG_TRY_INT(rec->begin("coop<" + std::to_string(k.n) + ">", 32.0 * k.pt_steps, st));
+            SHG_CUDA(launch_coop(k.n, d_desc_, list, bar, d_counters_ + 63, st));
+            if (rec) SHG_TRY_INT(rec->end(st));
+            return SHG_OK;
+        }
         if (k.resident) {
             int *counter = d_counters_ + ci;
             if (rec) SHG_TRY_INT(rec->begin("resident<" + std::to_string(k.n) + ">", 32.0 * k.pt_steps, st));
@@ -1271,6 +1321,7 @@ int shg_cwes(shg_handle *h, float temp) {
     h->sp.tprop = temp;
     SHG_TRY(handle_run(h, h->stream));
     SHG_CUDA(cudaStreamSynchronize(h->stream));
+    if (!h->th) SHG_TRY(h->batch.check_run_errors());
     return SHG_OK;
 }
 
@@ -1339,6 +1390,7 @@ int shg_run(shg_handle *h, float power, float waist, float focalpoint, float tem
     h->batch.set_slices(0, per_slice ? h->slices : nullptr);
     SHG_TRY(handle_run(h, h->stream));
     SHG_CUDA(cudaStreamSynchronize(h->stream));
+    if (!h->th) SHG_TRY(h->batch.check_run_errors());
     if (!h->out_dir.empty()) SHG_TRY(write_outputs(h, save_only_last, false));
     return SHG_OK;
 }
@@ -1353,6 +1405,7 @@ int shg_get_fields(shg_handle *h, float *pump_out, float *sh_out) {
     const InstDesc &d = h->batch.desc(0);
     const size_t bytes = (size_t)h->n * h->n * sizeof(float2);
     SHG_CUDA(cudaStreamSynchronize(h->stream));
+    SHG_TRY(h->batch.check_run_errors());
     if (pump_out) SHG_CUDA(cudaMemcpy(pump_out, d.Pout, bytes, cudaMemcpyDeviceToHost));
     if (sh_out) SHG_CUDA(cudaMemcpy(sh_out, d.Sout, bytes, cudaMemcpyDeviceToHost));
     return SHG_OK;
@@ -1607,7 +1660,10 @@ int shg_batch_run(shg_batch *b, double *eta, float *sh_out_all) {
         SHG_CUDA(cudaMemcpyAsync(sh_out_all, b->batch.sout_all(), b->batch.total_points() * sizeof(float2),
                                  cudaMemcpyDeviceToHost, b->stream));
     SHG_CUDA(cudaStreamSynchronize(b->stream));
-    if (eta) SHG_TRY(shg_batch_results(b, eta));
+    if (eta)
+        SHG_TRY(shg_batch_results(b, eta));
+    else
+        SHG_TRY(b->batch.check_run_errors());
     return SHG_OK;
 }
 
@@ -1617,6 +1673,7 @@ int shg_batch_fields(shg_batch *b, float *pump_out_all, float *sh_out_all) {
         return SHG_ERR_STATE;
     }
     SHG_CUDA(cudaStreamSynchronize(b->stream));
+    SHG_TRY(b->batch.check_run_errors());
     const size_t bytes = b->batch.total_points() * sizeof(float2);
     if (pump_out_all) SHG_CUDA(cudaMemcpy(pump_out_all, b->batch.pout_all(), bytes, cudaMemcpyDeviceToHost));
     if (sh_out_all) SHG_CUDA(cudaMemcpy(sh_out_all, b->batch.sout_all(), bytes, cudaMemcpyDeviceToHost));

@@ -21,7 +21,8 @@ const float2 *twiddle_symbol_address_resident256();
 
 // shg_march_v1.cu (resident march): variants (cluster size, CTAs per SM) per grid size
 struct ResidentVariant {
-    int cs, minb, g;  // cluster size, CTAs per SM, threads per line (FFT split N = (N/g) x g)
+    int cs, minb, g;  // cluster size, CTAs per SM, threads per line (FFT split N = (N/g) x g);
+                      // cs == 0: the persistent cooperative grid of one solve (launch_coop)
 };
 int resident_variants(int n, ResidentVariant *out, int max_out);
 ResidentVariant resident_default(int n);
@@ -33,6 +34,11 @@ cudaError_t launch_resident(int n, ResidentVariant v, const InstDesc *inst, cons
 cudaError_t launch_setup(const InstDesc *inst, int n_inst, int max_nn, int max_nz, cudaStream_t st);
 cudaError_t launch_rows(int n, const InstDesc *inst, const int *list, int count, int s, cudaStream_t st);
 cudaError_t launch_cols(int n, const InstDesc *inst, const int *list, int count, cudaStream_t st);
+// The whole march of one solve (list[0]) as one cooperative launch with bounded grid
+// barriers (bar: two zeroed words; err: zeroed, set to 1 when a barrier wait gave up).
+// inst == nullptr only checks that the grid fits co-resident; blocks receives its size.
+cudaError_t launch_coop(int n, const InstDesc *inst, const int *list, unsigned *bar, int *err, cudaStream_t st,
+                        int *blocks = nullptr);
 bool line_length_supported(int n);
 cudaError_t launch_dft2d(int n, int sign, const float2 *in, float2 *out, cudaStream_t st);
 cudaError_t launch_dft_rows(int n, int sign, const float2 *in, float2 *out, cudaStream_t st, int fields = 1);

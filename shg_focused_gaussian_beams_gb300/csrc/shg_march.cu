@@ -209,27 +209,27 @@ struct PtRowShape {
     static_assert(FT % 32 == 0 && 2 * FT <= TPB && N % LPB == 0, "transform threads fill whole warps");
 };
 
+// The row pass of k_rows_pt for lines [line0, line0 + LPB) of solve d at stage s, on a block
+// of PtRowShape<N>::TPB threads (shared by the streaming launch and the persistent grid).
 template <int N>
-__global__ void __launch_bounds__(PtRowShape<N>::TPB) k_rows_pt(const InstDesc *__restrict__ inst, const int *__restrict__ list, int s) {
+__device__ __forceinline__ void rows_pt_body(const InstDesc &d, int line0, int s, float2 *scratch, float2 *lines0,
+                                             float2 *lines1) {
     using Sh = PtRowShape<N>;
-    constexpr int G = Sh::G, E = N / G, LPB = Sh::LPB, BPI = Sh::BPI, FT = Sh::FT;
+    constexpr int G = Sh::G, E = N / G, LPB = Sh::LPB, FT = Sh::FT;
     constexpr int SC = LineScratch<N, G>::SIZE;
-    __shared__ float2 scratch[2 * LPB * SC];
-    __shared__ float2 lines[2][LPB * N];  // [field][line * N + x], natural x order
-    const InstDesc &d = inst[list[blockIdx.x / BPI]];
     const float2 *__restrict__ tab = g_twiddle + N;
-    const int tid = threadIdx.x, line0 = (blockIdx.x % BPI) * LPB;
+    const int tid = threadIdx.x;
     // transform role
     const bool xf = tid < 2 * FT;
     const int f = tid / FT, fl = (tid % FT) / G, t = tid % G;
     float2 *const F = f == 0 ? d.P : d.S;
-    float2 *const fline = lines[f & 1] + fl * N;
+    float2 *const fline = ((f & 1) ? lines1 : lines0) + fl * N;
     float2 *const fsc = scratch + (size_t)((f & 1) * LPB + fl) * SC;
     const size_t fbase = (size_t)(line0 + fl) * N;
     // point role
     const int l = tid / N, x = tid % N;
     const size_t i2 = (size_t)(line0 + l) * N + x;
-    float2 *const pP = lines[0] + l * N + x, *const pS = lines[1] + l * N + x;
+    float2 *const pP = lines0 + l * N + x, *const pS = lines1 + l * N + x;
 
     if (s == 0) {
         float2 vp = d.P[i2], vs = d.S[i2];
@@ -284,18 +284,22 @@ __global__ void __launch_bounds__(PtRowShape<N>::TPB) k_rows_pt(const InstDesc *
     }
 }
 
-// Column pass. Block = TC columns x G threads (lane = column + TC * t) so that every
-// load and store is a run of TC consecutive complex values; blockIdx.y = field (pump, SH).
-template <int N, int TC>
-__global__ void __launch_bounds__(TC * LineShape<N>::G) k_cols(const InstDesc *__restrict__ inst, const int *__restrict__ list) {
-    constexpr int G = LineShape<N>::G, E = N / G, BPI = N / TC;
-    __shared__ float2 scratch[TC * E * G];
-    const InstDesc &d = inst[list[blockIdx.x / BPI]];
+template <int N>
+__global__ void __launch_bounds__(PtRowShape<N>::TPB) k_rows_pt(const InstDesc *__restrict__ inst, const int *__restrict__ list, int s) {
+    using Sh = PtRowShape<N>;
+    __shared__ float2 scratch[2 * Sh::LPB * LineScratch<N, Sh::G>::SIZE];
+    __shared__ float2 lines[2][Sh::LPB * N];  // [field][line * N + x], natural x order
+    rows_pt_body<N>(inst[list[blockIdx.x / Sh::BPI]], (blockIdx.x % Sh::BPI) * Sh::LPB, s, scratch, lines[0],
+                    lines[1]);
+}
+
+// The column pass of k_cols for column x of field f (0 pump, 1 SH) of solve d, lane t of the
+// column's G lanes; the TC columns of a group transpose through sc (interleaved, stride TC)
+// and synchronise the block (BS) or, when the group is one warp, the warp.
+template <int N, int TC, bool BS>
+__device__ __forceinline__ void cols_body(const InstDesc &d, int x, int f, int t, float2 *sc) {
+    constexpr int G = LineShape<N>::G, E = N / G;
     const float2 *__restrict__ tab = g_twiddle + N;
-    const int c = threadIdx.x % TC, t = threadIdx.x / TC;
-    const int x = (blockIdx.x % BPI) * TC + c;
-    float2 *sc = scratch + c;
-    const int f = blockIdx.y;
     float2 *F = f == 0 ? d.P : d.S;
     const float2 *__restrict__ H = f == 0 ? d.Hp : d.Hs;
     // propagator values first: their latency overlaps the transform
@@ -304,12 +308,153 @@ __global__ void __launch_bounds__(TC * LineShape<N>::G) k_cols(const InstDesc *_
     float2 v[E];
 #pragma unroll
     for (int j = 0; j < E; ++j) v[j] = F[(size_t)(t + G * j) * N + x];
-    fft_nat_to_spec<N, G, +1, true, TC, G>(v, t, sc, tab);
+    fft_nat_to_spec<N, G, +1, BS, TC, G>(v, t, sc, tab);
 #pragma unroll
     for (int r = 0; r < E; ++r) v[r] = c_mul(v[r], h[r]);
-    fft_spec_to_nat<N, G, -1, true, TC, G>(v, t, sc, tab);
+    fft_spec_to_nat<N, G, -1, BS, TC, G>(v, t, sc, tab);
 #pragma unroll
     for (int j = 0; j < E; ++j) F[(size_t)(t + G * j) * N + x] = v[j];
+}
+
+// Column pass. Block = TC columns x G threads (lane = column + TC * t) so that every
+// load and store is a run of TC consecutive complex values; blockIdx.y = field (pump, SH).
+template <int N, int TC>
+__global__ void __launch_bounds__(TC * LineShape<N>::G) k_cols(const InstDesc *__restrict__ inst, const int *__restrict__ list) {
+    constexpr int G = LineShape<N>::G, E = N / G, BPI = N / TC;
+    __shared__ float2 scratch[TC * E * G];
+    const int c = threadIdx.x % TC;
+    cols_body<N, TC, true>(inst[list[blockIdx.x / BPI]], (blockIdx.x % BPI) * TC + c, blockIdx.y, threadIdx.x / TC,
+                           scratch + c);
+}
+
+// ---------------------------------------------------------------------------------------
+// Persistent march of one solve on a cooperative grid: the row and column passes of the
+// streaming kernels (rows_pt_body, cols_body: the same arithmetic, bit-identical results)
+// in one launch, separated by grid-wide barriers instead of kernel boundaries. A lone solve
+// otherwise pays two dependent launches per z-step.
+
+// Poll limit of a grid-barrier wait (~1 s with the back-off below).
+constexpr long long kGridWaitLimit = 1ll << 22;
+
+// Grid-wide barrier of a cooperative launch: bar[0] counts arrivals, bar[1] is the
+// generation. Every wait is bounded: on timeout *err is set and false is returned (the
+// caller leaves the kernel). The fences order each block's global writes before its arrival
+// and the other blocks' writes before this block's later loads.
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *vgen = bar + 1;
+        const unsigned gen = *vgen;
+        __threadfence();
+        int good = 1;
+        if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            for (long long it = 0; *vgen == gen; ++it) {
+                if (it >= kGridWaitLimit || *(volatile int *)err) {
+                    atomicExch(err, 1);
+                    good = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+template <int N>
+struct CoopShape {
+    static constexpr int G = LineShape<N>::G;
+    static constexpr int TPB = PtRowShape<N>::TPB;
+    static constexpr int TC = 32 / G;                    // columns per column group (one warp)
+    static constexpr int ROW_UNITS = PtRowShape<N>::BPI;  // groups of LPB lines
+    static constexpr int COL_UNITS = 2 * (N / TC);       // column groups of both fields
+    static_assert(TC * G == 32, "a column group is one warp");
+};
+
+// Grid of B blocks of TPB threads; block b runs row units b, b + B, ... and column groups
+// b + B w (warp w < col_warps). Dynamic shared memory: col_warps scratch regions of TC * N
+// float2. bar: two zeroed words; err: zeroed error word of the run.
+template <int N>
+__global__ void __launch_bounds__(CoopShape<N>::TPB) k_march_coop(const InstDesc *__restrict__ inst,
+                                                                 const int *__restrict__ list, unsigned *bar,
+                                                                 int *err, int col_warps) {
+    using Sh = PtRowShape<N>;
+    using C = CoopShape<N>;
+    constexpr int G = Sh::G;
+    __shared__ float2 scratch[2 * Sh::LPB * LineScratch<N, G>::SIZE];
+    __shared__ float2 lines[2][Sh::LPB * N];
+    extern __shared__ float2 cscr[];
+    const InstDesc &d = inst[list[0]];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int K = d.nsteps;
+    for (int s = 0; s <= K; ++s) {
+        for (int u = blockIdx.x; u < C::ROW_UNITS; u += gridDim.x) {
+            rows_pt_body<N>(d, u * Sh::LPB, s, scratch, lines[0], lines[1]);
+            __syncthreads();  // the block's line buffers are reused by its next unit
+        }
+        if (s == K) break;
+        if (!grid_barrier(bar, err)) return;
+        if (warp < col_warps) {
+            const int u = blockIdx.x + gridDim.x * warp;
+            if (u < C::COL_UNITS) {
+                const int f = u / (N / C::TC), x0 = (u % (N / C::TC)) * C::TC, c = lane % C::TC;
+                cols_body<N, C::TC, false>(d, x0 + c, f, lane / C::TC, cscr + (size_t)warp * C::TC * N + c);
+            }
+        }
+        if (!grid_barrier(bar, err)) return;
+    }
+}
+
+template <int N>
+static cudaError_t launch_coop_t(const InstDesc *inst, const int *list, unsigned *bar, int *err, cudaStream_t st,
+                                 int *blocks_out) {
+    using C = CoopShape<N>;
+    constexpr int warps = C::TPB / 32;
+    int blocks = C::ROW_UNITS;
+    if ((C::COL_UNITS + warps - 1) / warps > blocks) blocks = (C::COL_UNITS + warps - 1) / warps;
+    const int col_warps = (C::COL_UNITS + blocks - 1) / blocks;
+    const size_t smem = (size_t)col_warps * C::TC * N * sizeof(float2);
+    auto k = k_march_coop<N>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0, per_sm = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, C::TPB, smem)) != cudaSuccess) return e;
+    if (per_sm * sms < blocks) return cudaErrorCooperativeLaunchTooLarge;
+    if (blocks_out) *blocks_out = blocks;
+    if (!inst) return cudaSuccess;  // fit check only
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(blocks, 1, 1);
+    cfg.blockDim = dim3(C::TPB, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, inst, list, bar, err, col_warps);
+}
+
+cudaError_t launch_coop(int n, const InstDesc *inst, const int *list, unsigned *bar, int *err, cudaStream_t st,
+                        int *blocks) {
+    switch (n) {
+        case 16: return launch_coop_t<16>(inst, list, bar, err, st, blocks);
+        case 32: return launch_coop_t<32>(inst, list, bar, err, st, blocks);
+        case 64: return launch_coop_t<64>(inst, list, bar, err, st, blocks);
+        case 128: return launch_coop_t<128>(inst, list, bar, err, st, blocks);
+        case 256: return launch_coop_t<256>(inst, list, bar, err, st, blocks);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 // ---------------------------------------------------------------------------------------

@@ -67,6 +67,11 @@ ResidentVariant resident_default(int n) {
 }
 
 cudaError_t prepare_resident(int n, ResidentVariant v, int *max_clusters) {
+    if (v.cs == 0) {  // the persistent cooperative grid of one solve: does it fit co-resident?
+        const cudaError_t e = launch_coop(n, nullptr, nullptr, nullptr, nullptr, nullptr);
+        *max_clusters = e == cudaSuccess ? 1 : 0;
+        return e;
+    }
     switch (n) {
         case 16: case 32: case 64: return prepare_resident_small(n, v.cs, v.minb, v.g, max_clusters);
         case 128: return prepare_resident_128(v.cs, v.minb, v.g, max_clusters);

@@ -280,8 +280,12 @@ class Sweep:
         check(lib().shg_batch_autotune(self._b, stream), "shg_batch_autotune")
 
     def set_schedule(self, n, resident=True, cluster_size=1, ctas_per_sm=1, threads_per_line=None):
-        """Fix the schedule of the grid-n class (streaming, or a resident variant, optionally
-        with its line-FFT split)."""
+        """Fix the schedule of the grid-n class: streaming (resident=False), a resident variant
+        (optionally with its line-FFT split), or resident="coop", the persistent cooperative
+        grid of a batch of one solve."""
+        if resident == "coop":
+            check(lib().shg_batch_set_schedule(self._b, int(n), 2, 0, 0), "shg_batch_set_schedule")
+            return
         if resident and threads_per_line:
             check(lib().shg_batch_set_schedule_split(self._b, int(n), int(cluster_size), int(ctas_per_sm),
                                                      int(threads_per_line)), "shg_batch_set_schedule_split")

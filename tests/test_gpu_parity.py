@@ -229,3 +229,47 @@ def test_schedule_list_from_environment(monkeypatch):
     assert "n=256 solves=1: untuned" in text
     sw.run()
     assert "untuned" not in sw.schedule()
+
+
+@pytest.mark.parametrize("n,nz", [(32, 40), (64, 60), (128, 100), (256, 48)])
+def test_persistent_grid_matches_streaming(n, nz):
+    """A batch of one solve on the persistent cooperative grid (the whole march in one
+    launch, grid-wide barriers between the row and column passes) gives the streaming
+    kernels' fields bit for bit, on repeated runs of the captured graph."""
+    inst = W.plain_instance(n, nz, 10.0, 2.84, 50.0)
+    ref = Sweep([inst], crystal=W.CRYSTAL_QPM50)
+    ref.set_schedule(n, resident=False)
+    eta_r, fr = ref.run(with_fields=True)
+    sw = Sweep([inst], crystal=W.CRYSTAL_QPM50)
+    sw.set_schedule(n, resident="coop")
+    assert "coop" in sw.schedule() and sw.launch_count() == 3
+    for _ in range(3):
+        eta, f = sw.run(with_fields=True)
+        for x, y in zip(f, fr):
+            assert np.array_equal(x, y)
+        # the power sums are double atomics: order-dependent in the last bits
+        np.testing.assert_allclose(eta, eta_r, rtol=1e-12, atol=0)
+    ref.close()
+    sw.close()
+
+
+def test_persistent_grid_is_offered_to_a_lone_solve_only(monkeypatch):
+    from shg_focused_gaussian_beams_gb300._lib import ShgError
+    insts = [W.plain_instance(64, 20, p, 2.84, 50.0) for p in (5.0, 10.0)]
+    sw = Sweep(insts, crystal=W.CRYSTAL_QPM50)
+    with pytest.raises(ShgError, match="UNSUPPORTED"):
+        sw.set_schedule(64, resident="coop")
+    sw.close()
+    monkeypatch.setenv("SHG_MARCH", "64:coop")
+    lone = Sweep(insts[:1], crystal=W.CRYSTAL_QPM50)
+    assert "coop" in lone.schedule()
+    two = Sweep(insts, crystal=W.CRYSTAL_QPM50)
+    assert "untuned" in two.schedule()
+    lone.close()
+    two.close()
+    # the autotuner times it among the candidates of a lone solve
+    monkeypatch.delenv("SHG_MARCH")
+    at = Sweep([W.plain_instance(128, 30, 10.0, 2.84, 50.0)], crystal=W.CRYSTAL_QPM50)
+    at.autotune()
+    assert "coop" in at.schedule()
+    at.close()
