@@ -636,7 +636,7 @@ def run_ours(args):
                  "thread_inst_per_pt_step": tr["thread_inst_per_pt_step"], "source": tr.get("inst_source"),
                  "peak_note": f"{props.multi_processor_count} SMs x 128 lanes x {sm_mhz:.0f} MHz (nominal issue rate)"}
     fp32 = None
-    if dom.startswith("resident<"):  # the whole step in one kernel
+    if dom.startswith(("resident<", "cluster<", "coop<")):  # the whole march in one kernel
         # flops of the method per grid-pt.z-step: 4 2D FFTs at 5 N log2 N, 2 propagator
         # products, 2 RK4 calls (20 log2(N^2) + 456; sincos not counted), against the nominal
         # FP32 rate (no measured FP32 peak exists): SMs x 128 lanes x 2 flop x SM clock

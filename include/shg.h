@@ -205,7 +205,9 @@ int shg_batch_launch_count(shg_batch *b, int *launches);
 int shg_batch_autotune(shg_batch *b, void *stream);
 /* Fixes the schedule of the class with grid n: resident = 0 streaming, resident = 2 the
  * persistent cooperative grid (a batch of one solve only; cluster_size and ctas_per_sm
- * unused), else the resident variant with cluster_size CTAs per cluster and ctas_per_sm
+ * unused), resident = 3 the cluster march (n in {64, 128, 256}: each solve in one cluster
+ * of 8 / 16 / 16 CTAs of 512 threads, one thread per point in the pointwise phase;
+ * cluster_size and ctas_per_sm unused), else the resident variant with cluster_size CTAs per cluster and ctas_per_sm
  * CTAs per SM (variants: n <= 32 (1, 1); n = 64 (1, 1), (1, 2), (2, 2), (2, 4); n = 128
  * (2, 1), (4, 1), (4, 2); n = 256 (8, 1), (16, 1), (16, 2)). SHG_ERR_UNSUPPORTED if the
  * variant does not exist or fit. */

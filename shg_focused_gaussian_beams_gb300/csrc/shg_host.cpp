@@ -182,7 +182,8 @@ int ensure_twiddles(int device) {
         }
     for (const float2 *addr : {twiddle_symbol_address_march(), twiddle_symbol_address_thermal(),
                                twiddle_symbol_address_adjoint(), twiddle_symbol_address_resident(),
-                               twiddle_symbol_address_resident128(), twiddle_symbol_address_resident256()}) {
+                               twiddle_symbol_address_resident128(), twiddle_symbol_address_resident256(),
+                               twiddle_symbol_address_cluster_pt()}) {
         void *p = const_cast<float2 *>(addr);
         if (!p) {
             set_error("twiddle table symbol unavailable");
@@ -194,10 +195,12 @@ int ensure_twiddles(int device) {
     return SHG_OK;
 }
 
-// Name of a class schedule: "streaming", "coop" (persistent grid) or "cs/minb/g".
+// Name of a class schedule: "streaming", "coop" (persistent grid), "cluster" (one cluster
+// per solve, one thread per point) or "cs/minb/g".
 std::string schedule_label(bool resident, const ResidentVariant &v) {
     if (!resident) return "streaming";
     if (v.cs == 0) return "coop";
+    if (v.cs == -1) return "cluster";
     return std::to_string(v.cs) + "/" + std::to_string(v.minb) + "/" + std::to_string(v.g);
 }
 
@@ -302,8 +305,9 @@ class Batch {
         }
         // schedule per class from SHG_MARCH: "auto" (default: the autotuner picks at the first
         // run), "streaming", "resident" (default variants), or a list "n:streaming" /
-        // "n:cs/minb" / "n:coop" per grid (e.g. "64:1/1,128:4/2,256:16/2"; unlisted grids:
-        // autotuner; "coop", the persistent cooperative grid, applies to a batch of one solve)
+        // "n:cs/minb" / "n:coop" / "n:cluster" per grid (e.g. "64:1/1,128:4/2,256:16/2";
+        // unlisted grids: autotuner; "coop", the persistent cooperative grid, applies to a
+        // batch of one solve; "cluster" runs each solve in one cluster of the cluster march)
         const char *mode = std::getenv("SHG_MARCH");
         const std::string m = mode ? mode : "auto";
         for (auto &c : classes_) {
@@ -327,6 +331,12 @@ class Batch {
                     if (classes_.size() == 1 && c.count == 1) {
                         c.resident = true;
                         c.var = ResidentVariant{0, 0, 0};
+                        c.tuned = true;
+                    }
+                } else if (v == "cluster") {
+                    if (cluster_pt_size(c.n) > 0) {
+                        c.resident = true;
+                        c.var = ResidentVariant{-1, 1, 0};
                         c.tuned = true;
                     }
                 } else if (std::sscanf(v.c_str(), "%d/%d/%d", &cs, &mb, &g) >= 2) {
@@ -509,6 +519,13 @@ class Batch {
                 else
                     cudaGetLastError();  // a variant that does not fit is skipped
             }
+            if (cluster_pt_size(c.n) > 0) {  // one cluster per solve, where the class fits in one wave
+                int mc = 0;
+                if (prepare_resident(c.n, ResidentVariant{-1, 1, 0}, &mc) == cudaSuccess && mc >= c.count)
+                    cands.push_back({true, ResidentVariant{-1, 1, 0}, mc});
+                else
+                    cudaGetLastError();
+            }
             if (lone_solve()) {  // one solve in the batch: the persistent cooperative grid as well
                 int mc = 0;
                 if (prepare_resident(c.n, ResidentVariant{0, 0, 0}, &mc) == cudaSuccess && mc > 0)
@@ -680,6 +697,17 @@ class Batch {
                 c.resident = true;
                 c.var = ResidentVariant{0, 0, 0};
                 c.max_clusters = 1;
+            } else if (resident == 3) {
+                int mc = 0;
+                if (cluster_pt_size(n) < 1 || prepare_resident(n, ResidentVariant{-1, 1, 0}, &mc) != cudaSuccess ||
+                    mc < 1) {
+                    cudaGetLastError();
+                    set_error("set_schedule: the cluster march runs grids 64, 128 and 256 where a cluster fits");
+                    return SHG_ERR_UNSUPPORTED;
+                }
+                c.resident = true;
+                c.var = ResidentVariant{-1, 1, 0};
+                c.max_clusters = mc;
             } else {
                 ResidentVariant vs[16];
                 const int nv = resident_variants(n, vs, 16);
@@ -747,6 +775,7 @@ class Batch {
             out += !c.tuned                      ? std::string("untuned")
                    : !c.resident                   ? std::string("streaming")
                    : c.var.cs == 0                 ? std::string("coop (persistent grid)")
+                   : c.var.cs == -1                ? std::string("cluster march")
                                                    : "resident cs=" + std::to_string(c.var.cs) + " minb=" +
                                                        std::to_string(c.var.minb) + " g=" + std::to_string(c.var.g);
             if (!c.trials.empty()) {
@@ -961,7 +990,8 @@ class Batch {
         }
         if (k.resident) {
             int *counter = d_counters_ + ci;
-            if (rec) SHG_TRY_INT(rec->begin("resident<" + std::to_string(k.n) + ">", 32.0 * k.pt_steps, st));
+            const char *kind = k.var.cs == -1 ? "cluster<" : "resident<";
+            if (rec) SHG_TRY_INT(rec->begin(kind + std::to_string(k.n) + ">", 32.0 * k.pt_steps, st));
             SHG_CUDA(launch_resident(k.n, k.var, d_desc_, list, k.count, counter, k.max_clusters, st));
             if (rec) SHG_TRY_INT(rec->end(st));
             return SHG_OK;

@@ -18,11 +18,14 @@ const float2 *twiddle_symbol_address_adjoint();
 const float2 *twiddle_symbol_address_resident();
 const float2 *twiddle_symbol_address_resident128();
 const float2 *twiddle_symbol_address_resident256();
+const float2 *twiddle_symbol_address_cluster_pt();
 
 // shg_march_v1.cu (resident march): variants (cluster size, CTAs per SM) per grid size
 struct ResidentVariant {
     int cs, minb, g;  // cluster size, CTAs per SM, threads per line (FFT split N = (N/g) x g);
-                      // cs == 0: the persistent cooperative grid of one solve (launch_coop)
+                      // cs == 0: the persistent cooperative grid of one solve (launch_coop);
+                      // cs == -1: one cluster per solve, one thread per point in the
+                      // pointwise phase (launch_cluster_pt)
 };
 int resident_variants(int n, ResidentVariant *out, int max_out);
 ResidentVariant resident_default(int n);
@@ -40,6 +43,14 @@ cudaError_t launch_cols(int n, const InstDesc *inst, const int *list, int count,
 cudaError_t launch_coop(int n, const InstDesc *inst, const int *list, unsigned *bar, int *err, cudaStream_t st,
                         int *blocks = nullptr);
 bool line_length_supported(int n);
+
+// shg_cluster_pt.cu: the march of each of `count` solves (list[0..count)) in one
+// thread-block cluster of cluster_pt_size(n) CTAs, both fields in the cluster's shared
+// memory (n in {64, 128, 256}). prepare_cluster_pt: once per device, outside any capture;
+// max_clusters receives how many clusters fit at once (0: none).
+int cluster_pt_size(int n);
+cudaError_t prepare_cluster_pt(int n, int *max_clusters);
+cudaError_t launch_cluster_pt(int n, const InstDesc *inst, const int *list, int count, cudaStream_t st);
 cudaError_t launch_dft2d(int n, int sign, const float2 *in, float2 *out, cudaStream_t st);
 cudaError_t launch_dft_rows(int n, int sign, const float2 *in, float2 *out, cudaStream_t st, int fields = 1);
 

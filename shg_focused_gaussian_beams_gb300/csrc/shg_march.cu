@@ -333,36 +333,39 @@ __global__ void __launch_bounds__(TC * LineShape<N>::G) k_cols(const InstDesc *_
 // in one launch, separated by grid-wide barriers instead of kernel boundaries. A lone solve
 // otherwise pays two dependent launches per z-step.
 
-// Poll limit of a grid-barrier wait (~1 s with the back-off below).
+// Poll limit of a grid-barrier wait (about a second).
 constexpr long long kGridWaitLimit = 1ll << 22;
 
-// Grid-wide barrier of a cooperative launch: bar[0] counts arrivals, bar[1] is the
-// generation. Every wait is bounded: on timeout *err is set and false is returned (the
-// caller leaves the kernel). The fences order each block's global writes before its arrival
-// and the other blocks' writes before this block's later loads.
-__device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err) {
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void red_release_gpu(unsigned *p, unsigned v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Grid-wide barrier of a cooperative launch on a monotonic arrival counter (zeroed before
+// the launch): barrier number e of the run completes once e * gridDim.x arrivals are in.
+// Thread 0 of each block arrives with a release add (ordering the block's writes, which the
+// block barrier made its own, before the arrival) and polls with acquire loads (ordering
+// the other blocks' writes before this block's later loads). No reset step: a waiter reads
+// one word. Every wait is bounded: on timeout *err is set and false is returned (the
+// caller leaves the kernel), and a wait also ends once another block has set *err.
+__device__ __forceinline__ bool grid_barrier(unsigned *count, unsigned target, int *err) {
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile unsigned *vgen = bar + 1;
-        const unsigned gen = *vgen;
-        __threadfence();
+        red_release_gpu(count, 1u);
         int good = 1;
-        if (atomicAdd(bar, 1u) == gridDim.x - 1) {
-            atomicExch(bar, 0u);
-            __threadfence();
-            atomicAdd(bar + 1, 1u);
-        } else {
-            for (long long it = 0; *vgen == gen; ++it) {
-                if (it >= kGridWaitLimit || *(volatile int *)err) {
-                    atomicExch(err, 1);
-                    good = 0;
-                    break;
-                }
-                __nanosleep(64);
+        for (long long it = 0; ld_acquire_gpu(count) < target; ++it) {
+            if (it >= kGridWaitLimit || *(volatile int *)err) {
+                atomicExch(err, 1);
+                good = 0;
+                break;
             }
+            if (it >= 64) __nanosleep(32);
         }
-        __threadfence();
         ok = good;
     }
     __syncthreads();
@@ -371,7 +374,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err) {
 
 template <int N>
 struct CoopShape {
-    static constexpr int G = LineShape<N>::G;
+    static constexpr int G = LineShape<N>::G, E = N / G;
     static constexpr int TPB = PtRowShape<N>::TPB;
     static constexpr int TC = 32 / G;                    // columns per column group (one warp)
     static constexpr int ROW_UNITS = PtRowShape<N>::BPI;  // groups of LPB lines
@@ -379,9 +382,28 @@ struct CoopShape {
     static_assert(TC * G == 32, "a column group is one warp");
 };
 
+// cols_body with the column's propagator values already in registers.
+template <int N, int TC>
+__device__ __forceinline__ void cols_body_h(const InstDesc &d, int x, int f, int t, float2 *sc,
+                                            const float2 (&h)[N / LineShape<N>::G]) {
+    constexpr int G = LineShape<N>::G, E = N / G;
+    const float2 *__restrict__ tab = g_twiddle + N;
+    float2 *F = f == 0 ? d.P : d.S;
+    float2 v[E];
+#pragma unroll
+    for (int j = 0; j < E; ++j) v[j] = F[(size_t)(t + G * j) * N + x];
+    fft_nat_to_spec<N, G, +1, false, TC, G>(v, t, sc, tab);
+#pragma unroll
+    for (int r = 0; r < E; ++r) v[r] = c_mul(v[r], h[r]);
+    fft_spec_to_nat<N, G, -1, false, TC, G>(v, t, sc, tab);
+#pragma unroll
+    for (int j = 0; j < E; ++j) F[(size_t)(t + G * j) * N + x] = v[j];
+}
+
 // Grid of B blocks of TPB threads; block b runs row units b, b + B, ... and column groups
-// b + B w (warp w < col_warps). Dynamic shared memory: col_warps scratch regions of TC * N
-// float2. bar: two zeroed words; err: zeroed error word of the run.
+// b + B w (warp w < col_warps), whose propagator values stay in registers for the whole run.
+// Dynamic shared memory: col_warps scratch regions of TC * N float2. bar: zeroed arrival
+// counter; err: zeroed error word of the run.
 template <int N>
 __global__ void __launch_bounds__(CoopShape<N>::TPB) k_march_coop(const InstDesc *__restrict__ inst,
                                                                  const int *__restrict__ list, unsigned *bar,
@@ -395,21 +417,23 @@ __global__ void __launch_bounds__(CoopShape<N>::TPB) k_march_coop(const InstDesc
     const InstDesc &d = inst[list[0]];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int K = d.nsteps;
+    const int u = blockIdx.x + gridDim.x * warp;
+    const bool colw = warp < col_warps && u < C::COL_UNITS;
+    const int f = u / (N / C::TC), x = (u % (N / C::TC)) * C::TC + lane % C::TC, t = lane / C::TC;
+    float2 h[C::E];
+    if (colw) hprop_load<N>(f == 0 ? d.Hp : d.Hs, x, t, h);
+    unsigned target = 0;
     for (int s = 0; s <= K; ++s) {
-        for (int u = blockIdx.x; u < C::ROW_UNITS; u += gridDim.x) {
-            rows_pt_body<N>(d, u * Sh::LPB, s, scratch, lines[0], lines[1]);
+        for (int r = blockIdx.x; r < C::ROW_UNITS; r += gridDim.x) {
+            rows_pt_body<N>(d, r * Sh::LPB, s, scratch, lines[0], lines[1]);
             __syncthreads();  // the block's line buffers are reused by its next unit
         }
         if (s == K) break;
-        if (!grid_barrier(bar, err)) return;
-        if (warp < col_warps) {
-            const int u = blockIdx.x + gridDim.x * warp;
-            if (u < C::COL_UNITS) {
-                const int f = u / (N / C::TC), x0 = (u % (N / C::TC)) * C::TC, c = lane % C::TC;
-                cols_body<N, C::TC, false>(d, x0 + c, f, lane / C::TC, cscr + (size_t)warp * C::TC * N + c);
-            }
-        }
-        if (!grid_barrier(bar, err)) return;
+        target += gridDim.x;
+        if (!grid_barrier(bar, target, err)) return;
+        if (colw) cols_body_h<N, C::TC>(d, x, f, t, cscr + (size_t)warp * C::TC * N + lane % C::TC, h);
+        target += gridDim.x;
+        if (!grid_barrier(bar, target, err)) return;
     }
 }
 
@@ -418,18 +442,30 @@ static cudaError_t launch_coop_t(const InstDesc *inst, const int *list, unsigned
                                  int *blocks_out) {
     using C = CoopShape<N>;
     constexpr int warps = C::TPB / 32;
-    int blocks = C::ROW_UNITS;
-    if ((C::COL_UNITS + warps - 1) / warps > blocks) blocks = (C::COL_UNITS + warps - 1) / warps;
-    const int col_warps = (C::COL_UNITS + blocks - 1) / blocks;
-    const size_t smem = (size_t)col_warps * C::TC * N * sizeof(float2);
     auto k = k_march_coop<N>;
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
     int dev = 0, sms = 0, per_sm = 0;
+    cudaError_t e;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, C::TPB, smem)) != cudaSuccess) return e;
-    if (per_sm * sms < blocks) return cudaErrorCooperativeLaunchTooLarge;
+    // one column group per block where that many blocks fit co-resident (the column pass
+    // then spreads over the most SMs), else the fewest blocks that hold every row unit
+    int blocks = 0, col_warps = 0;
+    size_t smem = 0;
+    for (int pass = 0; pass < 2 && !blocks; ++pass) {
+        int b = C::ROW_UNITS;
+        if (pass == 0 && C::COL_UNITS > b) b = C::COL_UNITS;
+        if ((C::COL_UNITS + warps - 1) / warps > b) b = (C::COL_UNITS + warps - 1) / warps;
+        const int cw = (C::COL_UNITS + b - 1) / b;
+        const size_t sm = (size_t)cw * C::TC * N * sizeof(float2);
+        if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) != cudaSuccess) return e;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, C::TPB, sm)) != cudaSuccess) return e;
+        if (per_sm * sms >= b) {
+            blocks = b;
+            col_warps = cw;
+            smem = sm;
+        }
+    }
+    if (!blocks) return cudaErrorCooperativeLaunchTooLarge;
     if (blocks_out) *blocks_out = blocks;
     if (!inst) return cudaSuccess;  // fit check only
     cudaLaunchAttribute attr[1];

@@ -72,6 +72,7 @@ cudaError_t prepare_resident(int n, ResidentVariant v, int *max_clusters) {
         *max_clusters = e == cudaSuccess ? 1 : 0;
         return e;
     }
+    if (v.cs == -1) return prepare_cluster_pt(n, max_clusters);
     switch (n) {
         case 16: case 32: case 64: return prepare_resident_small(n, v.cs, v.minb, v.g, max_clusters);
         case 128: return prepare_resident_128(v.cs, v.minb, v.g, max_clusters);
@@ -82,6 +83,7 @@ cudaError_t prepare_resident(int n, ResidentVariant v, int *max_clusters) {
 
 cudaError_t launch_resident(int n, ResidentVariant v, const InstDesc *inst, const int *list, int njobs, int *counter,
                             int max_clusters, cudaStream_t st) {
+    if (v.cs == -1) return launch_cluster_pt(n, inst, list, njobs, st);  // one cluster per solve
     switch (n) {
         case 16: case 32: case 64:
             return launch_resident_small(n, v.cs, v.minb, v.g, inst, list, njobs, counter, max_clusters, st);

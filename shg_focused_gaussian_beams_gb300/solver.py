@@ -281,10 +281,12 @@ class Sweep:
 
     def set_schedule(self, n, resident=True, cluster_size=1, ctas_per_sm=1, threads_per_line=None):
         """Fix the schedule of the grid-n class: streaming (resident=False), a resident variant
-        (optionally with its line-FFT split), or resident="coop", the persistent cooperative
-        grid of a batch of one solve."""
-        if resident == "coop":
-            check(lib().shg_batch_set_schedule(self._b, int(n), 2, 0, 0), "shg_batch_set_schedule")
+        (optionally with its line-FFT split), resident="coop", the persistent cooperative
+        grid of a batch of one solve, or resident="cluster", one thread-block cluster per solve
+        with one thread per point in the pointwise phase."""
+        if resident in ("coop", "cluster"):
+            mode = 2 if resident == "coop" else 3
+            check(lib().shg_batch_set_schedule(self._b, int(n), mode, 0, 0), "shg_batch_set_schedule")
             return
         if resident and threads_per_line:
             check(lib().shg_batch_set_schedule_split(self._b, int(n), int(cluster_size), int(ctas_per_sm),

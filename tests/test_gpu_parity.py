@@ -273,3 +273,25 @@ def test_persistent_grid_is_offered_to_a_lone_solve_only(monkeypatch):
     at.autotune()
     assert "coop" in at.schedule()
     at.close()
+
+
+@pytest.mark.parametrize("n,nzs", [(64, [60]), (128, [100]), (256, [48]), (128, [40, 25, 40]), (64, [30, 20])])
+def test_cluster_march_matches_streaming(n, nzs):
+    """The cluster march (one cluster per solve, both fields in the cluster's shared memory,
+    one thread per point in the pointwise phase) gives the streaming kernels' fields bit for
+    bit, for a lone solve and for a batch of solves of different lengths, on repeated runs of
+    the captured graph."""
+    insts = [W.plain_instance(n, nz, 10.0 + 5.0 * i, 2.84, 50.0 + 0.5 * i) for i, nz in enumerate(nzs)]
+    ref = Sweep(insts, crystal=W.CRYSTAL_QPM50)
+    ref.set_schedule(n, resident=False)
+    eta_r, fr = ref.run(with_fields=True)
+    sw = Sweep(insts, crystal=W.CRYSTAL_QPM50)
+    sw.set_schedule(n, resident="cluster")
+    assert "cluster march" in sw.schedule() and sw.launch_count() == 3
+    for _ in range(2):
+        eta, f = sw.run(with_fields=True)
+        for x, y in zip(f, fr):
+            assert np.array_equal(x, y)
+        np.testing.assert_allclose(eta, eta_r, rtol=1e-12, atol=0)
+    ref.close()
+    sw.close()
