@@ -6,7 +6,8 @@
 // (N = E * G, x = t + G*j on input):
 //
 //   stage 1: each thread runs an E-point DFT over its registers (compile-time twiddles),
-//   twiddle:  multiply by w_N^(t*k2) from a table evaluated in double and rounded once,
+//   twiddle:  multiply by w_N^(t*k2) from a table evaluated in double and rounded once
+//             (stored per split as 16-byte pairs, see g_twiddle),
 //   transpose through shared memory,
 //   stage 2: each thread runs E/G DFTs of G points.
 //
@@ -29,11 +30,25 @@ namespace shg {
 
 constexpr int kMaxLine = 256;
 
-// Twiddle tables exp(-2 pi i m / N) for N = 16..kMaxLine: the table for line length N
-// sits at [N, 2N). Each translation unit that launches line FFTs has its own copy
-// (internal linkage) and registers its address with twiddle_tables_register(); the host
-// fills every registered copy once per device.
-static __device__ float2 g_twiddle[2 * kMaxLine];
+// Threads per line for each supported line length (E = N/G points per thread).
+template <int N>
+struct LineShape;
+template <> struct LineShape<16> { static constexpr int G = 4; };
+template <> struct LineShape<32> { static constexpr int G = 4; };
+template <> struct LineShape<64> { static constexpr int G = 8; };
+template <> struct LineShape<128> { static constexpr int G = 8; };
+template <> struct LineShape<256> { static constexpr int G = 16; };
+template <> struct LineShape<512> { static constexpr int G = 16; };
+
+// Inter-stage twiddles w_N^(t*k2) = exp(-2 pi i (t*k2 mod N) / N) of the split N = E x G,
+// for N = 16..kMaxLine, stored as 16-byte pairs: word (j*G + t) holds the twiddles of
+// k2 = 2j and 2j+1 for thread t (j < E/2), so the E - 1 twiddles of a thread take E/2
+// vector loads and the lanes of consecutive t read consecutive words. The table of line
+// length N for the default split G = LineShape<N>::G sits at float2 offset [N, 2N), the
+// one for G = LineShape<N>::G / 2 (N >= 64) at [2*kMaxLine + N, 2*kMaxLine + 2N). Each
+// translation unit that launches line FFTs has its own copy (internal linkage) whose
+// address the host looks up; the host fills every copy once per device.
+static __device__ __align__(16) float2 g_twiddle[4 * kMaxLine];
 
 __device__ __forceinline__ float2 c_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 c_sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
@@ -122,11 +137,20 @@ __device__ __forceinline__ void dft_reg(float2 (&v)[NV]) {
     sfor<E>([&](auto I) { v[OFF + decltype(I)::value] = t[decltype(I)::value]; });
 }
 
-// Twiddle w_N^m for direction SIGN from a table tab[m] = exp(-2 pi i m / N).
-template <int SIGN>
-__device__ __forceinline__ float2 tw_table(const float2 *__restrict__ tab, int m) {
-    const float2 w = __ldg(tab + m);
-    return SIGN > 0 ? make_float2(w.x, -w.y) : w;
+// Inter-stage twiddle multiply of thread t: v[k2] *= w_N^(SIGN-direction t*k2), k2 >= 1,
+// from the pair table of split (N, G). tab: the line length's block g_twiddle + N.
+template <int N, int G, int SIGN>
+__device__ __forceinline__ void twiddle_mul(float2 (&v)[N / G], int t, const float2 *__restrict__ tab) {
+    constexpr int E = N / G;
+    static_assert(G == LineShape<N>::G || (N >= 64 && 2 * G == LineShape<N>::G), "no twiddle table for this split");
+    const float4 *__restrict__ w4 =
+        reinterpret_cast<const float4 *>(G == LineShape<N>::G ? tab : tab + 2 * kMaxLine) + t;
+#pragma unroll
+    for (int j = 0; j < E / 2; ++j) {
+        const float4 q = __ldg(w4 + j * G);  // SIGN = +1 uses the conjugates
+        if (j > 0) v[2 * j] = c_mul(v[2 * j], make_float2(q.x, SIGN > 0 ? -q.y : q.y));
+        v[2 * j + 1] = c_mul(v[2 * j + 1], make_float2(q.z, SIGN > 0 ? -q.w : q.w));
+    }
 }
 
 // Per-line shared scratch: E rows of G entries padded to G+1, plus a line pad.
@@ -159,8 +183,7 @@ __device__ __forceinline__ void fft_nat_to_spec(float2 (&v)[N / G], int t, float
     constexpr int E = N / G, Q = E / G;
     static_assert(E % G == 0, "need G <= E with G | E");
     dft_reg<E, SIGN>(v);
-#pragma unroll
-    for (int k2 = 1; k2 < E; ++k2) v[k2] = c_mul(v[k2], tw_table<SIGN>(tab, (t * k2) & (N - 1)));
+    twiddle_mul<N, G, SIGN>(v, t, tab);
     group_sync<BS>();
 #pragma unroll
     for (int k2 = 0; k2 < E; ++k2) sc[(k2 * GP + t) * STRIDE] = v[k2];
@@ -186,8 +209,7 @@ __device__ __forceinline__ void fft_spec_to_nat(float2 (&v)[N / G], int t, float
     group_sync<BS>();
 #pragma unroll
     for (int k2 = 0; k2 < E; ++k2) v[k2] = sc[(k2 * GP + t) * STRIDE];
-#pragma unroll
-    for (int k2 = 1; k2 < E; ++k2) v[k2] = c_mul(v[k2], tw_table<SIGN>(tab, (t * k2) & (N - 1)));
+    twiddle_mul<N, G, SIGN>(v, t, tab);
     dft_reg<E, SIGN>(v);
 }
 
@@ -198,16 +220,6 @@ __device__ __forceinline__ int spec_index(int t, int r) {
     const int m = r / G, k1 = r % G;
     return (t * Q + m) + E * k1;
 }
-
-// Threads per line for each supported line length (E = N/G points per thread).
-template <int N>
-struct LineShape;
-template <> struct LineShape<16> { static constexpr int G = 4; };
-template <> struct LineShape<32> { static constexpr int G = 4; };
-template <> struct LineShape<64> { static constexpr int G = 8; };
-template <> struct LineShape<128> { static constexpr int G = 8; };
-template <> struct LineShape<256> { static constexpr int G = 16; };
-template <> struct LineShape<512> { static constexpr int G = 16; };
 
 // Propagator storage order. The column transforms (G = LineShape<N>::G threads per column,
 // E = N / G registers each) multiply register r of thread t by the propagator of spectral

@@ -168,18 +168,31 @@ int device_fits(size_t bytes, const char *what) {
     return SHG_OK;
 }
 
-// Twiddle tables exp(-2 pi i m/N), N = 16..256, at [N, 2N) of the device symbol.
+// Inter-stage twiddle tables of the line FFTs (layout at g_twiddle in shg_fft.cuh): for
+// N = 16..256 and the splits G = line_threads(N) (at [N, 2N)) and G / 2 for N >= 64 (at
+// [2*kMaxLine + N, 2*kMaxLine + 2N)), float2 2*(j*G + t) + b holds w_N^(t*(2j + b)),
+// w_N^m = exp(-2 pi i m/N) evaluated in double and rounded once.
 int ensure_twiddles(int device) {
     static std::mutex mu;
     static std::map<int, bool> done;
     std::lock_guard<std::mutex> lock(mu);
     if (done[device]) return SHG_OK;
-    std::vector<float2> tab(2 * kMaxLine, make_float2(0.f, 0.f));
-    for (int N = 16; N <= kMaxLine; N *= 2)
-        for (int m = 0; m < N; ++m) {
-            const double a = 2.0 * 3.14159265358979323846264338327950288 * (double)m / (double)N;
-            tab[N + m] = make_float2((float)std::cos(a), (float)(-std::sin(a)));
+    std::vector<float2> tab(4 * kMaxLine, make_float2(0.f, 0.f));
+    for (int N = 16; N <= kMaxLine; N *= 2) {
+        auto w = [N](int m) {
+            const double a = 2.0 * 3.14159265358979323846264338327950288 * (double)(m % N) / (double)N;
+            return make_float2((float)std::cos(a), (float)(-std::sin(a)));
+        };
+        for (int split = 0; split < (N >= 64 ? 2 : 1); ++split) {
+            const int G = line_threads(N) >> split, E = N / G;
+            float2 *dst = tab.data() + split * 2 * kMaxLine + N;
+            for (int j = 0; j < E / 2; ++j)
+                for (int t = 0; t < G; ++t) {
+                    dst[2 * (j * G + t)] = w(t * 2 * j);
+                    dst[2 * (j * G + t) + 1] = w(t * (2 * j + 1));
+                }
         }
+    }
     for (const float2 *addr : {twiddle_symbol_address_march(), twiddle_symbol_address_thermal(),
                                twiddle_symbol_address_adjoint(), twiddle_symbol_address_resident(),
                                twiddle_symbol_address_resident128(), twiddle_symbol_address_resident256(),
