@@ -248,6 +248,18 @@ int shg_batch_profile(shg_batch *b, shg_kernel_stat *stats, int max_stats, int *
 int shg_cwes_noalloc(const shg_config *cfg, float temp, const void *pump_in, const void *sh_in,
                      void *pump_out, void *sh_out, double *eta, void *stream);
 
+/* ---- Check build (no counterpart in the reference) ----------------------------------- */
+/* *enabled = 1 in the library built with device-side index checks (build.py variant
+ * "check": descriptors, stages, field / propagator / slice / voxel indices, cluster ranks,
+ * TMA box coordinates), else 0. A failed check never traps: it records its site and value
+ * and skips the access. This call synchronises the device, then reads and clears the first
+ * failure of every kernel translation unit: *site = 0 for none, else the check site
+ * (kChk* in csrc/shg_check.cuh), *value the offending index or value. */
+int shg_check_status(int *enabled, int *site, long long *value);
+/* Check build only: a kernel that touches no memory records (site 1, value), showing that a
+ * failure reaches shg_check_status. SHG_ERR_UNSUPPORTED in other builds. */
+int shg_check_selftest(long long value);
+
 /* ---- Batched gradient of the THERMAL z-march (fixed temperature fields) ----------- */
 /* No counterpart in the reference (its THERMAL Solver::run, Solver.h:287-340, is forward
  * only). `count` solves on one grid (cfg: NX = NY a power of two in [16, 256]; the

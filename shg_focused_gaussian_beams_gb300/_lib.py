@@ -9,7 +9,8 @@ import ctypes as C
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "libshg_gb300.so")
+# SHG_LIB selects another build of the same C ABI (the check or sanitizer variants of build.py)
+LIB_PATH = os.environ.get("SHG_LIB") or os.path.join(HERE, "_build", "libshg_gb300.so")
 
 _i, _f, _d = C.c_int, C.c_float, C.c_double
 _pf, _pd, _pi, _vp = C.POINTER(C.c_float), C.POINTER(C.c_double), C.POINTER(C.c_int), C.c_void_p
@@ -96,6 +97,8 @@ SIGNATURES = {
     "shg_thgrad_gradient": (_i, [_vp, _vp, _i, _vp, _pd, _pd, _vp]),
     "shg_thgrad_launch_count": (_i, [_vp]),
     "shg_thgrad_device_bytes": (C.c_double, [_vp]),
+    "shg_check_status": (_i, [_pi, _pi, C.POINTER(C.c_longlong)]),
+    "shg_check_selftest": (_i, [C.c_longlong]),
 }
 
 _lib = None

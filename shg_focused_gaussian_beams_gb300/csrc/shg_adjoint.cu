@@ -24,6 +24,7 @@ const float2 *twiddle_symbol_address_adjoint() {
     cudaGetSymbolAddress(&p, g_twiddle);
     return static_cast<const float2 *>(p);
 }
+SHG_CHECK_TU(adjoint)
 
 // Column pass of the diffraction step on one field of one solve (after the row transform
 // along x with sign +1): backward transform along y, then either
@@ -168,6 +169,9 @@ __global__ void __launch_bounds__(AdjRowShape<N>::TPB)
     __shared__ float2 scratch[2 * Cx::LPB * Cx::SC];
     __shared__ float2 lines[2][Cx::LPB * N];
     const InstDesc &d = *dd;
+    if (!SHG_REQUIRE(d.n == N && (!finish || (s >= 1 && s - 1 < d.nz)) && (!start || (s >= 0 && s < d.nz)),
+                     kChkAdjoint, s))
+        return;  // block-uniform
     const float2 *__restrict__ tab = g_twiddle + N;
     const size_t nn = (size_t)N * N;
     Cx cx(lines, scratch);
@@ -220,6 +224,9 @@ __global__ void __launch_bounds__(AdjRowShape<N>::TPB)
     __shared__ float2 scratch[2 * Cx::LPB * Cx::SC];
     __shared__ float2 lines[2][Cx::LPB * N];
     const InstDesc &d = *dd;
+    if (!SHG_REQUIRE(d.n == N && (!finish || (s + 1 >= 0 && s + 1 < d.nz)) && (!start || (s >= 0 && s < d.nz)),
+                     kChkAdjoint, s))
+        return;  // block-uniform
     const float2 *__restrict__ tab = g_twiddle + N;
     const size_t nn = (size_t)N * N;
     const float hp = d.hp, t0 = d.tpa0, t1 = d.tpa1, w6 = d.dz6;

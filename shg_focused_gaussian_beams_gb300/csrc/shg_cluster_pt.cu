@@ -28,6 +28,7 @@ const float2 *twiddle_symbol_address_cluster_pt() {
     cudaGetSymbolAddress(&p, g_twiddle);
     return static_cast<const float2 *>(p);
 }
+SHG_CHECK_TU(cluster_pt)
 
 template <int N>
 struct CptCluster;
@@ -78,6 +79,8 @@ __global__ void __launch_bounds__(CptShape<N>::TPB, 1)
     cg::cluster_group cluster = cg::this_cluster();
     const int rank = (int)cluster.block_rank();
     const InstDesc &d = inst[list[blockIdx.x / Sh::CS]];
+    // every CTA of the cluster reads the same descriptor: all leave before the first barrier
+    if (!SHG_REQUIRE(d.n == N && d.nsteps >= 1 && d.nsteps < d.nz, kChkDescriptor, d.n)) return;
     const int tid = threadIdx.x, K = d.nsteps;
     const size_t row0 = (size_t)rank * R * N;  // this CTA's first point in the N x N field
 
@@ -149,13 +152,13 @@ __global__ void __launch_bounds__(CptShape<N>::TPB, 1)
                 float2 p = sP[i], q = sS[i];
                 rk4_point(p, q, cprev, d);
                 if (d.slices && s < d.nz) {
-                    float2 *sl = d.slices + (size_t)s * 2 * N * N + row0;
-                    sl[i] = p;
-                    sl[(size_t)N * N + i] = q;
+                    float2 *sl = d.slices + (size_t)s * 2 * N * N;
+                    SHG_AT(sl, row0 + i, (size_t)2 * N * N, kChkSlices) = p;
+                    SHG_AT(sl, (size_t)N * N + row0 + i, (size_t)2 * N * N, kChkSlices) = q;
                 }
                 if (s == K) {
-                    d.Pout[row0 + i] = p;
-                    d.Sout[row0 + i] = q;
+                    SHG_AT(d.Pout, row0 + i, (size_t)N * N, kChkClusterPtRow) = p;
+                    SHG_AT(d.Sout, row0 + i, (size_t)N * N, kChkClusterPtRow) = q;
                     aS += (double)q.x * q.x + (double)q.y * q.y;
                     aP += (double)p.x * p.x + (double)p.y * p.y;
                 } else {
@@ -182,22 +185,23 @@ __global__ void __launch_bounds__(CptShape<N>::TPB, 1)
         // every CTA's rows are finished before any column is read
         cluster.sync();
         // ---- column phase on columns [rank R, rank R + R) of both fields (k_cols' arithmetic)
+        // element y of this thread's column: rank y / R, local row y % R (checked build:
+        // a bad element is redirected to this CTA's own first entry)
+        auto col_at = [&](int y) -> float2 * {
+            int rk = y / R, li = (y % R) * N + cx;
+            if (!SHG_REQUIRE(rk < Sh::CS && li < FIELD, kChkClusterPtCol, y)) rk = rank, li = 0;
+            return cluster.map_shared_rank(cfield + li, rk);
+        };
         if (xf) {
             float2 v[E];
 #pragma unroll
-            for (int j = 0; j < E; ++j) {
-                const int y = ct + G * j;
-                v[j] = *cluster.map_shared_rank(cfield + (y % R) * N + cx, y / R);
-            }
+            for (int j = 0; j < E; ++j) v[j] = *col_at(ct + G * j);
             fft_nat_to_spec<N, G, +1, false, TC, G>(v, ct, csc, tab);
 #pragma unroll
             for (int r = 0; r < E; ++r) v[r] = c_mul(v[r], h[r]);
             fft_spec_to_nat<N, G, -1, false, TC, G>(v, ct, csc, tab);
 #pragma unroll
-            for (int j = 0; j < E; ++j) {
-                const int y = ct + G * j;
-                *cluster.map_shared_rank(cfield + (y % R) * N + cx, y / R) = v[j];
-            }
+            for (int j = 0; j < E; ++j) *col_at(ct + G * j) = v[j];
         }
         // every column is written back before any row is read again
         cluster.sync();

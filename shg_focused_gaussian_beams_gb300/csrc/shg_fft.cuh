@@ -26,6 +26,8 @@
 
 #include <utility>
 
+#include "shg_check.cuh"
+
 namespace shg {
 
 constexpr int kMaxLine = 256;
@@ -254,7 +256,7 @@ __device__ __forceinline__ void hprop_load(const float2 *__restrict__ H, int x, 
     const float4 *p = reinterpret_cast<const float4 *>(H);
 #pragma unroll
     for (int j = 0; j < E / 2; ++j) {
-        const float4 q = __ldg(p + ((size_t)t * (E / 2) + j) * N + x);
+        const float4 q = __ldg(&SHG_AT(p, ((size_t)t * (E / 2) + j) * N + x, (size_t)N * N / 2, kChkPropagator));
         h[2 * j] = make_float2(q.x, q.y);
         h[2 * j + 1] = make_float2(q.z, q.w);
     }

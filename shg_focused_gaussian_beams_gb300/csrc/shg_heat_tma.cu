@@ -113,6 +113,9 @@ __global__ void __launch_bounds__(THREADS) k_heat_tma(float *__restrict__ Tf, co
                 if (i >= SLOTS && !mbar_wait(&empty[s], ((i / SLOTS) - 1) & 1, err)) break;
                 mbar_expect_tx(&full[s], G::T_BYTES + G::Q_BYTES);
                 const int p = z0 - 1 + i;
+                // the box's x start must be a 16-byte boundary (4 floats): a copy that would
+                // start off it is not issued (its waits then run out and report)
+                if (!SHG_REQUIRE(((x0 - XOFF) & 3) == 0 && (x0 & 3) == 0, kChkHeatTmaCoord, x0)) break;
                 tma_load_3d(sT + s * TS, &mT, x0 - XOFF, y0 - 1, p, &full[s]);
                 tma_load_3d(sQ + s * QS, &mQ, x0, y0, p, &full[s]);
                 issued = i + 1;
@@ -149,13 +152,15 @@ __global__ void __launch_bounds__(THREADS) k_heat_tma(float *__restrict__ Tf, co
             const float zm = sT[sm * TS + k], zp = sT[sp * TS + k];
             const float qk = sQ[s0 * QS + (warp + CONSUMER_WARPS * r) * TX + lane];
             if (in[r]) {
+                const long long vi = (long long)z * sxy + (long long)y * nx + x;
                 if (colint[r] && zint) {
-                    Tf[z * sxy + y * nx + x] = interior_voxel(c, P[k - 1], P[k + 1], P[k - BX], P[k + BX], zm, zp, qk);
+                    SHG_AT(Tf, vi, (long long)sxy * nz, kChkHeatVoxel) =
+                        interior_voxel(c, P[k - 1], P[k + 1], P[k - BX], P[k + BX], zm, zp, qk);
                 } else {
                     float v;
                     if (heat_voxel<BC>(c, x, y, z, nx, ny, nz, P[k - 1], P[k + 1], P[k - BX], P[k + BX], zm, zp, qk,
                                        v))
-                        Tf[z * sxy + y * nx + x] = v;
+                        SHG_AT(Tf, vi, (long long)sxy * nz, kChkHeatVoxel) = v;
                 }
             }
         }
@@ -214,6 +219,8 @@ cudaError_t tensor_map(const float *base, int nx, int ny, int nz, int bx, int by
 }
 
 }  // namespace
+
+SHG_CHECK_TU(heat_tma)
 
 // Planes per block: a block streams its chunk plus one halo plane on each side. At
 // 256x256x400 on GB300 with 4 rows per warp, chunks of 4, 6, 8, 16, 32 planes take 71.2,

@@ -1847,6 +1847,45 @@ int shg_batch_schedule(shg_batch *b, char *buf, int len) {
     return (int)s.size() < len ? SHG_OK : SHG_ERR_INVALID;
 }
 
+int shg_check_status(int *enabled, int *site, long long *value) {
+    if (!enabled || !site || !value) {
+        set_error("null argument");
+        return SHG_ERR_INVALID;
+    }
+    *enabled = kCheckBuild ? 1 : 0;
+    *site = 0;
+    *value = 0;
+    if (!kCheckBuild) return SHG_OK;
+    SHG_CUDA(cudaDeviceSynchronize());
+    unsigned long long first = 0;
+    for (auto take : {check_word_take_march, check_word_take_resident64, check_word_take_resident128,
+                      check_word_take_resident256, check_word_take_cluster_pt, check_word_take_thermal,
+                      check_word_take_heat_tma, check_word_take_adjoint}) {
+        const unsigned long long w = take();
+        if (w == ~0ull) {
+            set_error("shg_check_status: status word unreadable");
+            return SHG_ERR_CUDA;
+        }
+        if (w && !first) first = w;
+    }
+    if (first) {
+        *site = (int)(first >> 48);
+        long long v = (long long)(first & 0xffffffffffffull);
+        if (v & (1ll << 47)) v -= 1ll << 48;  // sign of the 48-bit value
+        *value = v;
+    }
+    return SHG_OK;
+}
+
+int shg_check_selftest(long long value) {
+    if (!kCheckBuild) {
+        set_error("shg_check_selftest: library built without SHG_CHECK");
+        return SHG_ERR_UNSUPPORTED;
+    }
+    SHG_CUDA(launch_check_selftest(value));
+    return SHG_OK;
+}
+
 int shg_dft2d_device(int n, int sign, const void *in, void *out, void *stream) {
     if (!line_length_supported(n) || (sign != 1 && sign != -1) || !in || !out) {
         set_error("shg_dft2d_device: unsupported size or bad argument");

@@ -20,6 +20,18 @@ const float2 *twiddle_symbol_address_resident128();
 const float2 *twiddle_symbol_address_resident256();
 const float2 *twiddle_symbol_address_cluster_pt();
 
+// Check build (shg_check.cuh): each kernel translation unit's first failed check, read and
+// cleared (0: none; ~0: unreadable); always 0 in other builds.
+unsigned long long check_word_take_march();
+unsigned long long check_word_take_resident64();
+unsigned long long check_word_take_resident128();
+unsigned long long check_word_take_resident256();
+unsigned long long check_word_take_cluster_pt();
+unsigned long long check_word_take_thermal();
+unsigned long long check_word_take_heat_tma();
+unsigned long long check_word_take_adjoint();
+cudaError_t launch_check_selftest(long long value);
+
 // shg_march_v1.cu (resident march): variants (cluster size, CTAs per SM) per grid size
 struct ResidentVariant {
     int cs, minb, g;  // cluster size, CTAs per SM, threads per line (FFT split N = (N/g) x g);

@@ -27,6 +27,23 @@ const float2 *twiddle_symbol_address_march() {
     cudaGetSymbolAddress(&p, g_twiddle);
     return static_cast<const float2 *>(p);
 }
+SHG_CHECK_TU(march)
+
+// Check build: the descriptor matches the kernel's grid and stage s is a valid SSFM stage.
+template <int N>
+__device__ __forceinline__ bool check_solve(const InstDesc &d, int s) {
+    return SHG_REQUIRE(d.n == N, kChkDescriptor, d.n) &&
+           SHG_REQUIRE(s >= 0 && s <= d.nsteps && d.nsteps < d.nz, kChkStage, s);
+}
+
+// Check-build self test: records (kChkSelfTest, value) without touching memory.
+__global__ void k_check_selftest(long long value) {
+    if (threadIdx.x == 0) SHG_REQUIRE(false, kChkSelfTest, value);
+}
+cudaError_t launch_check_selftest(long long value) {
+    k_check_selftest<<<1, 32>>>(value);
+    return cudaGetLastError();
+}
 
 // ---------------------------------------------------------------------------------------
 // Setup: phase table, Gaussian pump, shifted propagators, input power.
@@ -130,6 +147,8 @@ __global__ void __launch_bounds__(RowShape<N>::TPB) k_rows(const InstDesc *__res
     static_assert(N % LPB == 0, "blocks must not straddle solves");
     __shared__ float2 scratch[LPB * SC];
     const InstDesc &d = inst[list[blockIdx.x / BPI]];
+    if (!check_solve<N>(d, s)) return;  // whole block (d and s are block-uniform)
+    constexpr size_t NN = (size_t)N * N;
     const float2 *__restrict__ tab = g_twiddle + N;
     const int line = (blockIdx.x % BPI) * LPB + threadIdx.x / G;
     const int t = threadIdx.x % G;
@@ -138,8 +157,8 @@ __global__ void __launch_bounds__(RowShape<N>::TPB) k_rows(const InstDesc *__res
     float2 vp[E], vs[E];
 #pragma unroll
     for (int j = 0; j < E; ++j) {
-        vp[j] = d.P[base + t + G * j];
-        vs[j] = d.S[base + t + G * j];
+        vp[j] = SHG_AT(d.P, base + t + G * j, NN, kChkRowsGlobal);
+        vs[j] = SHG_AT(d.S, base + t + G * j, NN, kChkRowsGlobal);
     }
     if (s == 0) {
         const float4 c = d.stepc[0];
@@ -150,8 +169,8 @@ __global__ void __launch_bounds__(RowShape<N>::TPB) k_rows(const InstDesc *__res
 #pragma unroll
         for (int r = 0; r < E; ++r) {
             const int k = spec_index<N, G>(t, r);
-            d.P[base + k] = vp[r];
-            d.S[base + k] = vs[r];
+            SHG_AT(d.P, base + k, NN, kChkRowsGlobal) = vp[r];
+            SHG_AT(d.S, base + k, NN, kChkRowsGlobal) = vs[r];
         }
         return;
     }
@@ -165,8 +184,8 @@ __global__ void __launch_bounds__(RowShape<N>::TPB) k_rows(const InstDesc *__res
 #pragma unroll
         for (int r = 0; r < E; ++r) {
             const int k = spec_index<N, G>(t, r);
-            sl[base + k] = vp[r];
-            sl[(size_t)N * N + base + k] = vs[r];
+            SHG_AT(sl, base + k, 2 * NN, kChkSlices) = vp[r];
+            SHG_AT(sl, NN + base + k, 2 * NN, kChkSlices) = vs[r];
         }
     }
     if (s == d.nsteps) {
@@ -174,8 +193,8 @@ __global__ void __launch_bounds__(RowShape<N>::TPB) k_rows(const InstDesc *__res
 #pragma unroll
         for (int r = 0; r < E; ++r) {
             const int k = spec_index<N, G>(t, r);
-            d.Pout[base + k] = vp[r];
-            d.Sout[base + k] = vs[r];
+            SHG_AT(d.Pout, base + k, NN, kChkRowsGlobal) = vp[r];
+            SHG_AT(d.Sout, base + k, NN, kChkRowsGlobal) = vs[r];
             aS += (double)vs[r].x * vs[r].x + (double)vs[r].y * vs[r].y;
             aP += (double)vp[r].x * vp[r].x + (double)vp[r].y * vp[r].y;
         }
@@ -190,8 +209,8 @@ __global__ void __launch_bounds__(RowShape<N>::TPB) k_rows(const InstDesc *__res
     fft_spec_to_nat<N, G, +1>(vs, t, sc, tab);
 #pragma unroll
     for (int j = 0; j < E; ++j) {
-        d.P[base + t + G * j] = vp[j];
-        d.S[base + t + G * j] = vs[j];
+        SHG_AT(d.P, base + t + G * j, NN, kChkRowsGlobal) = vp[j];
+        SHG_AT(d.S, base + t + G * j, NN, kChkRowsGlobal) = vs[j];
     }
 }
 
@@ -230,6 +249,8 @@ __device__ __forceinline__ void rows_pt_body(const InstDesc &d, int line0, int s
     const int l = tid / N, x = tid % N;
     const size_t i2 = (size_t)(line0 + l) * N + x;
     float2 *const pP = lines0 + l * N + x, *const pS = lines1 + l * N + x;
+    constexpr size_t NN = (size_t)N * N;
+    if (!SHG_REQUIRE(line0 >= 0 && line0 + LPB <= N, kChkRowsGlobal, line0)) return;  // block-uniform
 
     if (s == 0) {
         float2 vp = d.P[i2], vs = d.S[i2];
@@ -289,8 +310,9 @@ __global__ void __launch_bounds__(PtRowShape<N>::TPB) k_rows_pt(const InstDesc *
     using Sh = PtRowShape<N>;
     __shared__ float2 scratch[2 * Sh::LPB * LineScratch<N, Sh::G>::SIZE];
     __shared__ float2 lines[2][Sh::LPB * N];  // [field][line * N + x], natural x order
-    rows_pt_body<N>(inst[list[blockIdx.x / Sh::BPI]], (blockIdx.x % Sh::BPI) * Sh::LPB, s, scratch, lines[0],
-                    lines[1]);
+    const InstDesc &d = inst[list[blockIdx.x / Sh::BPI]];
+    if (!check_solve<N>(d, s)) return;  // whole block
+    rows_pt_body<N>(d, (blockIdx.x % Sh::BPI) * Sh::LPB, s, scratch, lines[0], lines[1]);
 }
 
 // The column pass of k_cols for column x of field f (0 pump, 1 SH) of solve d, lane t of the
@@ -302,18 +324,19 @@ __device__ __forceinline__ void cols_body(const InstDesc &d, int x, int f, int t
     const float2 *__restrict__ tab = g_twiddle + N;
     float2 *F = f == 0 ? d.P : d.S;
     const float2 *__restrict__ H = f == 0 ? d.Hp : d.Hs;
+    constexpr size_t NN = (size_t)N * N;
     // propagator values first: their latency overlaps the transform
     float2 h[E];
     hprop_load<N>(H, x, t, h);
     float2 v[E];
 #pragma unroll
-    for (int j = 0; j < E; ++j) v[j] = F[(size_t)(t + G * j) * N + x];
+    for (int j = 0; j < E; ++j) v[j] = SHG_AT(F, (size_t)(t + G * j) * N + x, NN, kChkColsGlobal);
     fft_nat_to_spec<N, G, +1, BS, TC, G>(v, t, sc, tab);
 #pragma unroll
     for (int r = 0; r < E; ++r) v[r] = c_mul(v[r], h[r]);
     fft_spec_to_nat<N, G, -1, BS, TC, G>(v, t, sc, tab);
 #pragma unroll
-    for (int j = 0; j < E; ++j) F[(size_t)(t + G * j) * N + x] = v[j];
+    for (int j = 0; j < E; ++j) SHG_AT(F, (size_t)(t + G * j) * N + x, NN, kChkColsGlobal) = v[j];
 }
 
 // Column pass. Block = TC columns x G threads (lane = column + TC * t) so that every
@@ -323,8 +346,9 @@ __global__ void __launch_bounds__(TC * LineShape<N>::G) k_cols(const InstDesc *_
     constexpr int G = LineShape<N>::G, E = N / G, BPI = N / TC;
     __shared__ float2 scratch[TC * E * G];
     const int c = threadIdx.x % TC;
-    cols_body<N, TC, true>(inst[list[blockIdx.x / BPI]], (blockIdx.x % BPI) * TC + c, blockIdx.y, threadIdx.x / TC,
-                           scratch + c);
+    const InstDesc &d = inst[list[blockIdx.x / BPI]];
+    if (!SHG_REQUIRE(d.n == N, kChkDescriptor, d.n)) return;
+    cols_body<N, TC, true>(d, (blockIdx.x % BPI) * TC + c, blockIdx.y, threadIdx.x / TC, scratch + c);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -389,15 +413,16 @@ __device__ __forceinline__ void cols_body_h(const InstDesc &d, int x, int f, int
     constexpr int G = LineShape<N>::G, E = N / G;
     const float2 *__restrict__ tab = g_twiddle + N;
     float2 *F = f == 0 ? d.P : d.S;
+    constexpr size_t NN = (size_t)N * N;
     float2 v[E];
 #pragma unroll
-    for (int j = 0; j < E; ++j) v[j] = F[(size_t)(t + G * j) * N + x];
+    for (int j = 0; j < E; ++j) v[j] = SHG_AT(F, (size_t)(t + G * j) * N + x, NN, kChkCoop);
     fft_nat_to_spec<N, G, +1, false, TC, G>(v, t, sc, tab);
 #pragma unroll
     for (int r = 0; r < E; ++r) v[r] = c_mul(v[r], h[r]);
     fft_spec_to_nat<N, G, -1, false, TC, G>(v, t, sc, tab);
 #pragma unroll
-    for (int j = 0; j < E; ++j) F[(size_t)(t + G * j) * N + x] = v[j];
+    for (int j = 0; j < E; ++j) SHG_AT(F, (size_t)(t + G * j) * N + x, NN, kChkCoop) = v[j];
 }
 
 // Grid of B blocks of TPB threads; block b runs row units b, b + B, ... and column groups
@@ -415,6 +440,8 @@ __global__ void __launch_bounds__(CoopShape<N>::TPB) k_march_coop(const InstDesc
     __shared__ float2 lines[2][Sh::LPB * N];
     extern __shared__ float2 cscr[];
     const InstDesc &d = inst[list[0]];
+    // every block of the grid leaves together (before its first barrier) on a bad descriptor
+    if (!check_solve<N>(d, 0)) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int K = d.nsteps;
     const int u = blockIdx.x + gridDim.x * warp;

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "shg_check.cuh"
 #include "shg_fft.cuh"
 
 namespace shg {

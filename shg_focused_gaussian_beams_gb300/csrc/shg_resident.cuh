@@ -78,6 +78,8 @@ __global__ void __launch_bounds__(ResShape<N, CS_, MINB_, G_>::THREADS, MINB_)
         cluster_barrier<CS>();
         if (job >= njobs) break;
         const InstDesc &d = inst[list[job]];
+        // a bad descriptor skips the job in every CTA of the cluster alike (no barrier inside)
+        if (!SHG_REQUIRE(d.n == N && d.nsteps < d.nz && d.nsteps >= 1, kChkDescriptor, job)) continue;
         // load this CTA's rows of both fields
         {
             const float4 *gP = reinterpret_cast<const float4 *>(d.P + (size_t)rank * FIELD);
@@ -122,12 +124,13 @@ __global__ void __launch_bounds__(ResShape<N, CS_, MINB_, G_>::THREADS, MINB_)
 #pragma unroll
                     for (int r = 0; r < E; ++r) rk4_point(vp[r], vs[r], c1, d);
                     if (d.slices && s < d.nz) {
-                        float2 *sl = d.slices + (size_t)s * 2 * N * N + (size_t)(rank * R + line) * N;
+                        float2 *sl = d.slices + (size_t)s * 2 * N * N;
+                        const size_t base = (size_t)(rank * R + line) * N;
 #pragma unroll
                         for (int r = 0; r < E; ++r) {
                             const int k = spec_index<N, G>(t, r);
-                            sl[k] = vp[r];
-                            sl[(size_t)N * N + k] = vs[r];
+                            SHG_AT(sl, base + k, (size_t)2 * N * N, kChkSlices) = vp[r];
+                            SHG_AT(sl, (size_t)N * N + base + k, (size_t)2 * N * N, kChkSlices) = vs[r];
                         }
                     }
                     if (s == K) {
@@ -136,8 +139,8 @@ __global__ void __launch_bounds__(ResShape<N, CS_, MINB_, G_>::THREADS, MINB_)
 #pragma unroll
                         for (int r = 0; r < E; ++r) {
                             const int k = spec_index<N, G>(t, r);
-                            d.Pout[base + k] = vp[r];
-                            d.Sout[base + k] = vs[r];
+                            SHG_AT(d.Pout, base + k, (size_t)N * N, kChkResidentLoad) = vp[r];
+                            SHG_AT(d.Sout, base + k, (size_t)N * N, kChkResidentLoad) = vs[r];
                             aS += (double)vs[r].x * vs[r].x + (double)vs[r].y * vs[r].y;
                             aP += (double)vp[r].x * vp[r].x + (double)vp[r].y * vp[r].y;
                         }
@@ -168,8 +171,10 @@ __global__ void __launch_bounds__(ResShape<N, CS_, MINB_, G_>::THREADS, MINB_)
                     const float2 *__restrict__ H = f == 0 ? d.Hp : d.Hs;
                     auto at = [&](int j) -> float2 * {
                         const int y = ct + G * j;
-                        float2 *p = F + (y % R) * N + x;
-                        if constexpr (CS > 1) p = cg::this_cluster().map_shared_rank(p, y / R);
+                        int rk = y / R, li = (y % R) * N + x;
+                        if (!SHG_REQUIRE(rk < CS && li < FIELD, kChkResidentCol, y)) rk = rank, li = 0;
+                        float2 *p = F + li;
+                        if constexpr (CS > 1) p = cg::this_cluster().map_shared_rank(p, rk);
                         return p;
                     };
                     // propagator values first: their L2 latency overlaps the column transform

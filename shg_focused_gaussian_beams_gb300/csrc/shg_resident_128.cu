@@ -8,6 +8,7 @@ const float2 *twiddle_symbol_address_resident128() {
     cudaGetSymbolAddress(&p, g_twiddle);
     return static_cast<const float2 *>(p);
 }
+SHG_CHECK_TU(resident128)
 
 SHG_RESIDENT_INSTANTIATE(128, 2, 1, 8)
 SHG_RESIDENT_INSTANTIATE(128, 4, 1, 8)

@@ -8,6 +8,7 @@ const float2 *twiddle_symbol_address_resident256() {
     cudaGetSymbolAddress(&p, g_twiddle);
     return static_cast<const float2 *>(p);
 }
+SHG_CHECK_TU(resident256)
 
 SHG_RESIDENT_INSTANTIATE(256, 8, 1, 16)
 SHG_RESIDENT_INSTANTIATE(256, 16, 1, 16)

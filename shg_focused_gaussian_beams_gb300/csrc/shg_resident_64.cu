@@ -8,6 +8,7 @@ const float2 *twiddle_symbol_address_resident() {
     cudaGetSymbolAddress(&p, g_twiddle);
     return static_cast<const float2 *>(p);
 }
+SHG_CHECK_TU(resident64)
 
 SHG_RESIDENT_INSTANTIATE(16, 1, 1, 4)
 SHG_RESIDENT_INSTANTIATE(32, 1, 1, 4)

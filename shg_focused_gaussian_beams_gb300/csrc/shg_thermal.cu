@@ -22,6 +22,7 @@ const float2 *twiddle_symbol_address_thermal() {
     cudaGetSymbolAddress(&p, g_twiddle);
     return static_cast<const float2 *>(p);
 }
+SHG_CHECK_TU(thermal)
 
 // ---------------------------------------------------------------------------------------
 // Tfield.h:31-110: T = Temp everywhere, then the oven faces (bc 0: y = 0 plane; bc 1: all
@@ -526,6 +527,8 @@ __global__ void __launch_bounds__(ThRowShape<N>::TPB) k_rows_th(const InstDesc *
     __shared__ float2 scratch[2 * LPB * SC];
     __shared__ float2 lines[2][LPB * N];  // [field][line * N + x], natural x order
     const InstDesc &d = *dd;
+    // stages 0..nz: the THERMAL march runs one stage past the last slice (heat source of slice nz-1)
+    if (!SHG_REQUIRE(d.n == N && s >= 0 && s <= th.nz && (int)blockIdx.x < Sh::BPI, kChkThermalRows, s)) return;
     const float2 *__restrict__ tab = g_twiddle + N;
     const size_t nxy = (size_t)N * N;
     const int tid = threadIdx.x;
@@ -585,7 +588,7 @@ __global__ void __launch_bounds__(ThRowShape<N>::TPB) k_rows_th(const InstDesc *
         const float a2s = fmaf(vs.x, vs.x, vs.y * vs.y);
         const float Ip = th.qc * np1 * a2p, Is = th.qc * ns1 * a2s;
         const float Q = th.alpha_p * Ip + th.alpha_s * Is + th.beta_s * (Is * Is);
-        th.QK[i3] = Q / th.kth;
+        SHG_AT(th.QK, i3, (size_t)th.nz * nxy, kChkThermalRows) = Q / th.kth;
         if (d.slices && s < th.nz) {
             float2 *sl = d.slices + (size_t)s * 2 * nxy;
             sl[i2] = vp;
