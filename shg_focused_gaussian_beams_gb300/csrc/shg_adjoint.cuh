@@ -123,4 +123,68 @@ __device__ __forceinline__ void rk4_vjp_point(float2 P, float2 S, float2 &cP, fl
     cS = c_add(cas, bs);
 }
 
+// Fused row passes for one solve, one thread per point (block = LPB lines x N threads; the
+// x-transforms of the pump and SH lines run on two groups of LPB * G threads). Between two
+// column passes a row pass finishes one diffraction along x, applies the pointwise RK4 (or
+// RK4^T) work of the step boundary, and starts the next diffraction along x, so a z-step
+// costs one row and one column launch. The working state A / cotangent C holds the pump
+// then the SH field (n*n each); the column passes (k_colpass) see rows in natural
+// frequency order, as after launch_dft_rows(+1).
+template <int N>
+struct AdjRowShape {
+    static constexpr int G = LineShape<N>::G;
+    static constexpr int LPB = (512 / N < N) ? 512 / N : N;
+    static constexpr int TPB = LPB * N;
+    static constexpr int BPI = N / LPB;
+    static constexpr int FT = LPB * G;  // transform threads per field
+    static_assert(FT % 32 == 0 && 2 * FT <= TPB && N % LPB == 0, "transform threads fill whole warps");
+};
+
+// Shared state of a fused row pass: line buffers and the roles of this thread.
+template <int N>
+struct AdjRowCtx {
+    using Sh = AdjRowShape<N>;
+    static constexpr int G = Sh::G, E = N / G, LPB = Sh::LPB, FT = Sh::FT, SC = LineScratch<N, G>::SIZE;
+    float2 *fline, *fsc;  // transform role: this thread's line buffer and FFT scratch
+    int t;
+    bool xf;
+    size_t frow;          // offset of the transformed row in A (field included)
+    size_t i2;            // point role: index of the point in one field
+    int lx;               // point role: offset in a line buffer
+    __device__ AdjRowCtx(float2 (*lines)[LPB * N], float2 *scratch) {
+        const int tid = threadIdx.x, line0 = blockIdx.x * LPB;
+        xf = tid < 2 * FT;
+        const int f = (tid / FT) & 1, fl = (tid % FT) / G;
+        t = tid % G;
+        fline = lines[f] + fl * N;
+        fsc = scratch + (size_t)(f * LPB + fl) * SC;
+        frow = (size_t)f * N * N + (size_t)(line0 + fl) * N;
+        const int l = tid / N, x = tid % N;
+        i2 = (size_t)(line0 + l) * N + x;
+        lx = l * N + x;
+    }
+    // rows of A (natural frequency order) -> line buffers in real space (natural x order)
+    __device__ void finish(const float2 *A, const float2 *tab) {
+        if (xf) {
+            float2 v[E];
+#pragma unroll
+            for (int j = 0; j < E; ++j) v[j] = A[frow + t + G * j];
+            fft_nat_to_spec<N, G, -1>(v, t, fsc, tab);
+#pragma unroll
+            for (int r = 0; r < E; ++r) fline[spec_index<N, G>(t, r)] = v[r];
+        }
+    }
+    // line buffers (real space) -> rows of A in natural frequency order
+    __device__ void start(float2 *A, const float2 *tab) {
+        if (xf) {
+            float2 v[E];
+#pragma unroll
+            for (int r = 0; r < E; ++r) v[r] = fline[spec_index<N, G>(t, r)];
+            fft_spec_to_nat<N, G, +1>(v, t, fsc, tab);
+#pragma unroll
+            for (int j = 0; j < E; ++j) A[frow + t + G * j] = v[j];
+        }
+    }
+};
+
 }  // namespace shg

@@ -80,6 +80,8 @@ class ThermalGradBatch {
     float2 *in_ = nullptr, *X_ = nullptr, *cot_ = nullptr, *ck_ = nullptr, *Xs_ = nullptr, *Ws_ = nullptr;
     double *sums_ = nullptr;      // [0, count) sum |S_out|^2, [count, 2 count) sum |P_in|^2
     cudaStream_t cap_ = nullptr;
+    cudaStream_t side_ = nullptr;  // replay branch of the checkpointed gradient graph
+    cudaEvent_t ev_ = nullptr;     // joins between the branches (capture time)
     cudaGraphExec_t g_fwd_ = nullptr, g_grad_ = nullptr;
     int g_grad_L_ = -1;
     bool g_grad_all_ = false;

@@ -43,6 +43,8 @@ namespace shg {
 ThermalGradBatch::~ThermalGradBatch() {
     drop_graphs();
     if (cap_) cudaStreamDestroy(cap_);
+    if (side_) cudaStreamDestroy(side_);
+    if (ev_) cudaEventDestroy(ev_);
     for (void *p : {(void *)T_, (void *)coef_, (void *)props_, (void *)pump0_, (void *)stepc_, (void *)setup_acc_,
                     (void *)seed_, (void *)d_desc_, work_})
         if (p) cudaFree(p);
@@ -169,15 +171,18 @@ int ThermalGradBatch::gaussian_pumps(float2 *dst, cudaStream_t st) {
     return SHG_OK;
 }
 
-// Layout of the work space: in (count*nn), X, cot (count*2nn each), nck checkpoints and L
-// states of each of X_s, W_s (count*2nn each), then 2*count doubles of sums.
+// Layout of the work space: in (count*nn), X, cot (count*2nn each), nck checkpoints and
+// `slots` states of each of X_s, W_s (count*2nn each; with checkpoints two sets of L, one
+// being replayed while the other is reversed; storing every step, L), then 2*count doubles
+// of sums.
 int ThermalGradBatch::ensure_work(int L, int nck) {
     if (work_ && L == L_ && nck == nck_) return SHG_OK;
     drop_graphs();
     if (work_) cudaFree(work_);
     work_ = nullptr;
     const size_t st = (size_t)count_ * 2 * nn_;
-    work_bytes_ = sizeof(float2) * ((size_t)count_ * nn_ + st * (2 + (size_t)nck + 2 * (size_t)L)) +
+    const size_t slots = (nck > 0 ? 2 : 1) * (size_t)L;
+    work_bytes_ = sizeof(float2) * ((size_t)count_ * nn_ + st * (2 + (size_t)nck + 2 * slots)) +
                   sizeof(double) * 2 * (size_t)count_;
     TG_TRY(device_fits(work_bytes_, "batched THERMAL gradient work space"));
     TG_CUDA(cudaMalloc(&work_, work_bytes_));
@@ -191,9 +196,9 @@ int ThermalGradBatch::ensure_work(int L, int nck) {
     ck_ = p;
     p += st * nck;
     Xs_ = p;
-    p += st * L;
+    p += st * slots;
     Ws_ = p;
-    p += st * L;
+    p += st * slots;
     sums_ = reinterpret_cast<double *>(p);
     L_ = L;
     nck_ = nck;
@@ -214,63 +219,98 @@ int ThermalGradBatch::enqueue(bool grad, int L, int nseg, bool store_all, cudaSt
     TG_CUDA(cudaMemset2DAsync(X_ + nn_, 2 * nn_ * sizeof(float2), 0, nn_ * sizeof(float2), B, st));
     TG_CUDA(launch_abs2_sum_b(X_, nn, 0, sums_ + B, B, st));
     ++nl;
-    auto diffraction = [&](float2 *A, int mode) -> int {
-        TG_CUDA(launch_dft_rows(n, +1, A, A, st, 2 * B));
-        TG_CUDA(launch_colpass(n, mode, A, nullptr, d_desc_, nullptr, st, B));
-        TG_CUDA(launch_dft_rows(n, -1, A, A, st, 2 * B));
+    auto diffraction = [&](float2 *A, int mode, cudaStream_t q) -> int {
+        TG_CUDA(launch_dft_rows(n, +1, A, A, q, 2 * B));
+        TG_CUDA(launch_colpass(n, mode, A, nullptr, d_desc_, nullptr, q, B));
+        TG_CUDA(launch_dft_rows(n, -1, A, A, q, 2 * B));
         nl += 3;
         return SHG_OK;
     };
     // Step boundary s (0 <= s <= K) of the forward march on X_: second RK4 of step s-1
     // (input W_{s-1} to save_w), X_s to save_x, first RK4 of step s; one pass per boundary.
-    auto boundary = [&](int s, int s_end, float2 *save_w, float2 *save_x) -> int {
-        TG_CUDA(launch_th_rk4_pair(X_, save_w, save_x, coef_, nn, K, s - 1, s < s_end ? s : -1, d_desc_, B, st));
+    auto boundary = [&](int s, int s_end, float2 *save_w, float2 *save_x, cudaStream_t q) -> int {
+        TG_CUDA(launch_th_rk4_pair(X_, save_w, save_x, coef_, nn, K, s - 1, s < s_end ? s : -1, d_desc_, B, q));
         ++nl;
         return SHG_OK;
     };
-    // forward from the inputs: checkpoints every L steps (store_all: X_s, W_s of every step)
+    // Checkpointed: segment seg's states go to slot set seg & 1 (replayed there, or, for the
+    // last two segments, written by the forward pass itself, which the two slot sets hold
+    // without a replay)
+    auto slot_set = [&](int seg) -> size_t { return (size_t)(seg & 1) * L * sz; };
+    auto stored = [&](int seg) -> bool { return !store_all && seg >= nseg - 2; };
+    // forward from the inputs: checkpoints every L steps (store_all: X_s, W_s of every step;
+    // checkpointed: X_s, W_s of the last two segments as well)
     auto save_x = [&](int s) -> float2 * {
         if (!grad || s >= K) return nullptr;
         if (store_all) return Xs_ + (size_t)s * sz;
+        if (stored(s / L)) return Xs_ + slot_set(s / L) + (size_t)(s % L) * sz;
         return s % L == 0 ? ck_ + (size_t)(s / L) * sz : nullptr;
     };
-    TG_TRY(boundary(0, K, nullptr, save_x(0)));
+    auto save_w = [&](int s) -> float2 * {
+        if (!grad) return nullptr;
+        if (store_all) return Ws_ + (size_t)s * sz;
+        return stored(s / L) ? Ws_ + slot_set(s / L) + (size_t)(s % L) * sz : nullptr;
+    };
+    TG_TRY(boundary(0, K, nullptr, save_x(0), st));
     for (int s = 0; s < K; ++s) {
-        TG_TRY(diffraction(X_, 0));
-        TG_TRY(boundary(s + 1, K, grad && store_all ? Ws_ + (size_t)s * sz : nullptr, save_x(s + 1)));
+        TG_TRY(diffraction(X_, 0, st));
+        TG_TRY(boundary(s + 1, K, save_w(s), save_x(s + 1), st));
     }
     TG_CUDA(launch_abs2_sum_b(X_, nn, nn, sums_, B, st));
     ++nl;
     if (!grad) return SHG_OK;
     TG_CUDA(launch_seed_b(X_, cot_, nn, seed_, B, st));
     ++nl;
-    for (int seg = nseg - 1; seg >= 0; --seg) {
-        const int s0 = store_all ? 0 : seg * L, s1 = store_all ? K : std::min(K, s0 + L);
-        if (!store_all) {
-            // replay the segment from its checkpoint, keeping X_s, W_s for s0 <= s < s1
-            TG_CUDA(cudaMemcpyAsync(X_, ck_ + (size_t)seg * sz, sz * sizeof(float2), cudaMemcpyDeviceToDevice, st));
-            TG_CUDA(launch_th_rk4_pair(X_, nullptr, Xs_, coef_, nn, K, -1, s0, d_desc_, B, st));
-            ++nl;
-            for (int s = s0; s < s1; ++s) {
-                TG_TRY(diffraction(X_, 0));
-                const size_t j = (size_t)(s - s0) * sz;
-                TG_TRY(boundary(s + 1, s1, Ws_ + j, s + 1 < s1 ? Xs_ + j + sz : nullptr));
-            }
-        }
-        // reverse: RK4^T at W_{s1-1}; then per step s the adjoint diffraction and one pass
-        // with RK4^T at X_s and at W_{s-1}
-        TG_CUDA(launch_th_vjp_pair(nullptr, Ws_ + (size_t)(s1 - 1 - s0) * sz, cot_, coef_, nn, K, -1, s1 - 1, d_desc_,
-                                   B, st));
+    // reverse sweep of steps [s0, s1) on `q` with the states X_s, W_s of those steps at
+    // Xs, Ws (slot s - s0): RK4^T at W_{s1-1}; then per step s the adjoint diffraction and
+    // one pass with RK4^T at X_s and at W_{s-1}
+    auto backward = [&](int s0, int s1, const float2 *Xs, const float2 *Ws, cudaStream_t q) -> int {
+        TG_CUDA(launch_th_vjp_pair(nullptr, Ws + (size_t)(s1 - 1 - s0) * sz, cot_, coef_, nn, K, -1, s1 - 1, d_desc_,
+                                   B, q));
         ++nl;
         for (int s = s1 - 1; s >= s0; --s) {
-            TG_TRY(diffraction(cot_, 2));
+            TG_TRY(diffraction(cot_, 2, q));
             const size_t j = (size_t)(s - s0) * sz;
             const bool more = s - 1 >= s0;
-            TG_CUDA(launch_th_vjp_pair(Xs_ + j, more ? Ws_ + j - sz : nullptr, cot_, coef_, nn, K, s, more ? s - 1 : -1,
-                                       d_desc_, B, st));
+            TG_CUDA(launch_th_vjp_pair(Xs + j, more ? Ws + j - sz : nullptr, cot_, coef_, nn, K, s, more ? s - 1 : -1,
+                                       d_desc_, B, q));
             ++nl;
         }
-        if (store_all) break;
+        return SHG_OK;
+    };
+    if (store_all) return backward(0, K, Xs_, Ws_, st);
+    // The other segments are replayed from their checkpoints on the side branch into their
+    // slot set (X_ is the replay's working state; the reverse sweep works on cot_), so the
+    // replay of segment seg-1 runs while segment seg is reversed on `st`.
+    auto replay = [&](int seg, cudaStream_t q) -> int {
+        const int s0 = seg * L, s1 = std::min(K, s0 + L);
+        float2 *Xs = Xs_ + slot_set(seg), *Ws = Ws_ + slot_set(seg);
+        TG_CUDA(cudaMemcpyAsync(X_, ck_ + (size_t)seg * sz, sz * sizeof(float2), cudaMemcpyDeviceToDevice, q));
+        TG_CUDA(launch_th_rk4_pair(X_, nullptr, Xs, coef_, nn, K, -1, s0, d_desc_, B, q));
+        ++nl;
+        for (int s = s0; s < s1; ++s) {
+            TG_TRY(diffraction(X_, 0, q));
+            const size_t j = (size_t)(s - s0) * sz;
+            TG_TRY(boundary(s + 1, s1, Ws + j, s + 1 < s1 ? Xs + j + sz : nullptr, q));
+        }
+        return SHG_OK;
+    };
+    // branch b waits for everything enqueued so far on branch a
+    auto join = [&](cudaStream_t a, cudaStream_t b) -> int {
+        TG_CUDA(cudaEventRecord(ev_, a));
+        TG_CUDA(cudaStreamWaitEvent(b, ev_, 0));
+        return SHG_OK;
+    };
+    for (int seg = nseg - 1; seg >= 0; --seg) {
+        if (!stored(seg)) TG_TRY(join(side_, st));  // replay(seg) done
+        // replay(seg-1) reuses the slot set of segment seg+1, whose reverse sweep st finished
+        // (and the seed has read the forward's final X_ before the first replay)
+        if (seg >= 1 && !stored(seg - 1)) {
+            TG_TRY(join(st, side_));
+            TG_TRY(replay(seg - 1, side_));
+        }
+        const int s0 = seg * L, s1 = std::min(K, s0 + L);
+        TG_TRY(backward(s0, s1, Xs_ + slot_set(seg), Ws_ + slot_set(seg), st));
     }
     return SHG_OK;
 }
@@ -353,6 +393,8 @@ int ThermalGradBatch::gradient(const float2 *pump_in, int checkpoints, float2 *g
     if (!g_grad_ || g_grad_L_ != L || g_grad_all_ != store_all) {
         if (g_grad_) cudaGraphExecDestroy(g_grad_);
         g_grad_ = nullptr;
+        if (!side_) TG_CUDA(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking));
+        if (!ev_) TG_CUDA(cudaEventCreateWithFlags(&ev_, cudaEventDisableTiming));
         TG_TRY(capture(cap_, &g_grad_, [&](cudaStream_t c) { return enqueue(true, L, nseg, store_all, c); }));
         g_grad_L_ = L;
         g_grad_all_ = store_all;
