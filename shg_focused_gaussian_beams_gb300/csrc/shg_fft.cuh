@@ -94,24 +94,42 @@ struct W32 {
                                     0.3826834261417389f, 0.19509032368659973f};
 };
 
-// b * exp(SIGN * 2 pi i M / 32), with the exact special cases M = 0, 4, 8, 12.
+// tan(pi m / 16) for m = 0..4, evaluated in double and rounded to float.
+struct TanPi16 {
+    static constexpr float t[5] = {0.0f, 0.19891236737965800691f, 0.41421356237309504880f, 0.66817863791929891999f,
+                                   1.0f};
+};
+
+// Radix-2 butterfly (x, y) -> (x + w y, x - w y), w = exp(SIGN * 2 pi i M / 32). A
+// non-trivial w y is formed as f * u with f = cos or sin of the angle (whichever is larger
+// in magnitude) and u = y rotated by the ratio of the other to it (|ratio| <= 1), so that
+// f multiplies inside the output FMAs: six instructions instead of eight for the
+// product-then-add form.
 template <int SIGN, int M>
-__device__ __forceinline__ float2 tw_const(float2 b) {
-    constexpr float r = 0.7071067690849304f;
+__device__ __forceinline__ void bfly_const(float2 &a, float2 &b) {
+    const float2 x = a, y = b;
     if constexpr (M == 0) {
-        return b;
+        a = c_add(x, y);
+        b = c_sub(x, y);
     } else if constexpr (M == 8) {
-        return SIGN > 0 ? make_float2(-b.y, b.x) : make_float2(b.y, -b.x);
-    } else if constexpr (M == 4) {
-        return SIGN > 0 ? make_float2((b.x - b.y) * r, (b.y + b.x) * r)
-                        : make_float2((b.x + b.y) * r, (b.y - b.x) * r);
-    } else if constexpr (M == 12) {
-        return SIGN > 0 ? make_float2(-(b.x + b.y) * r, (b.x - b.y) * r)
-                        : make_float2((b.y - b.x) * r, -(b.x + b.y) * r);
-    } else {
+        const float2 wy = SIGN > 0 ? make_float2(-y.y, y.x) : make_float2(y.y, -y.x);
+        a = c_add(x, wy);
+        b = c_sub(x, wy);
+    } else if constexpr (M <= 4 || M >= 12) {
+        // w y = c (y.x - tau y.y, y.y + tau y.x), tau = SIGN tan(angle), |tau| <= 1
         constexpr float c = W32::c[M];
-        constexpr float s = SIGN > 0 ? W32::s[M] : -W32::s[M];
-        return make_float2(fmaf(b.x, c, -b.y * s), fmaf(b.x, s, b.y * c));
+        constexpr float tau = (SIGN > 0 ? 1.0f : -1.0f) * (M <= 4 ? TanPi16::t[M] : -TanPi16::t[16 - M]);
+        const float ux = fmaf(-tau, y.y, y.x), uy = fmaf(tau, y.x, y.y);
+        a = make_float2(fmaf(c, ux, x.x), fmaf(c, uy, x.y));
+        b = make_float2(fmaf(-c, ux, x.x), fmaf(-c, uy, x.y));
+    } else {
+        // w y = s (kappa y.x - y.y, kappa y.y + y.x), s = SIGN sin(angle), kappa = SIGN cot(angle)
+        constexpr float sg = SIGN > 0 ? 1.0f : -1.0f;
+        constexpr float s = sg * W32::s[M];
+        constexpr float kappa = sg * (M < 8 ? TanPi16::t[8 - M] : -TanPi16::t[M - 8]);
+        const float ux = fmaf(kappa, y.x, -y.y), uy = fmaf(kappa, y.y, y.x);
+        a = make_float2(fmaf(s, ux, x.x), fmaf(s, uy, x.y));
+        b = make_float2(fmaf(-s, ux, x.x), fmaf(-s, uy, x.y));
     }
 }
 
@@ -130,10 +148,7 @@ __device__ __forceinline__ void dft_reg(float2 (&v)[NV]) {
         sfor<E / 2>([&](auto B) {
             constexpr int grp = decltype(B)::value / half, k = decltype(B)::value % half;
             constexpr int a = grp * len + k, b = a + half;
-            const float2 y = tw_const<SIGN, k * (32 / len)>(t[b]);
-            const float2 x = t[a];
-            t[a] = c_add(x, y);
-            t[b] = c_sub(x, y);
+            bfly_const<SIGN, k * (32 / len)>(t[a], t[b]);
         });
     });
     sfor<E>([&](auto I) { v[OFF + decltype(I)::value] = t[decltype(I)::value]; });
