@@ -154,17 +154,23 @@ __device__ __forceinline__ void dft_reg(float2 (&v)[NV]) {
     sfor<E>([&](auto I) { v[OFF + decltype(I)::value] = t[decltype(I)::value]; });
 }
 
+// The pair table of split (N, G) within the line length's block tab = g_twiddle + N.
+template <int N, int G>
+__device__ __forceinline__ const float2 *twiddle_split(const float2 *tab) {
+    static_assert(G == LineShape<N>::G || (N >= 64 && 2 * G == LineShape<N>::G), "no twiddle table for this split");
+    return G == LineShape<N>::G ? tab : tab + 2 * kMaxLine;
+}
+
 // Inter-stage twiddle multiply of thread t: v[k2] *= w_N^(SIGN-direction t*k2), k2 >= 1,
-// from the pair table of split (N, G). tab: the line length's block g_twiddle + N.
-template <int N, int G, int SIGN>
+// from the pair table of split (N, G). tab: the line length's block g_twiddle + N, or with
+// TS a copy of the split's own table (N float2) in shared memory.
+template <int N, int G, int SIGN, bool TS = false>
 __device__ __forceinline__ void twiddle_mul(float2 (&v)[N / G], int t, const float2 *__restrict__ tab) {
     constexpr int E = N / G;
-    static_assert(G == LineShape<N>::G || (N >= 64 && 2 * G == LineShape<N>::G), "no twiddle table for this split");
-    const float4 *__restrict__ w4 =
-        reinterpret_cast<const float4 *>(G == LineShape<N>::G ? tab : tab + 2 * kMaxLine) + t;
+    const float4 *__restrict__ w4 = reinterpret_cast<const float4 *>(TS ? tab : twiddle_split<N, G>(tab)) + t;
 #pragma unroll
     for (int j = 0; j < E / 2; ++j) {
-        const float4 q = __ldg(w4 + j * G);  // SIGN = +1 uses the conjugates
+        const float4 q = TS ? w4[j * G] : __ldg(w4 + j * G);  // SIGN = +1 uses the conjugates
         if (j > 0) v[2 * j] = c_mul(v[2 * j], make_float2(q.x, SIGN > 0 ? -q.y : q.y));
         v[2 * j + 1] = c_mul(v[2 * j + 1], make_float2(q.z, SIGN > 0 ? -q.w : q.w));
     }
@@ -195,12 +201,12 @@ __device__ __forceinline__ void group_sync() {
 // GP = G + 1 and a padded per-line base; lines interleaved across lanes (column passes)
 // use STRIDE = lines per block, GP = G and base = scratch + line.
 // L_in -> DFT in L_out.
-template <int N, int G, int SIGN, bool BS = false, int STRIDE = 1, int GP = G + 1>
+template <int N, int G, int SIGN, bool BS = false, int STRIDE = 1, int GP = G + 1, bool TS = false>
 __device__ __forceinline__ void fft_nat_to_spec(float2 (&v)[N / G], int t, float2 *sc, const float2 *__restrict__ tab) {
     constexpr int E = N / G, Q = E / G;
     static_assert(E % G == 0, "need G <= E with G | E");
     dft_reg<E, SIGN>(v);
-    twiddle_mul<N, G, SIGN>(v, t, tab);
+    twiddle_mul<N, G, SIGN, TS>(v, t, tab);
     group_sync<BS>();
 #pragma unroll
     for (int k2 = 0; k2 < E; ++k2) sc[(k2 * GP + t) * STRIDE] = v[k2];
@@ -213,7 +219,7 @@ __device__ __forceinline__ void fft_nat_to_spec(float2 (&v)[N / G], int t, float
 }
 
 // L_out -> DFT in L_in.
-template <int N, int G, int SIGN, bool BS = false, int STRIDE = 1, int GP = G + 1>
+template <int N, int G, int SIGN, bool BS = false, int STRIDE = 1, int GP = G + 1, bool TS = false>
 __device__ __forceinline__ void fft_spec_to_nat(float2 (&v)[N / G], int t, float2 *sc, const float2 *__restrict__ tab) {
     constexpr int E = N / G, Q = E / G;
     static_assert(E % G == 0, "need G <= E with G | E");
@@ -226,7 +232,7 @@ __device__ __forceinline__ void fft_spec_to_nat(float2 (&v)[N / G], int t, float
     group_sync<BS>();
 #pragma unroll
     for (int k2 = 0; k2 < E; ++k2) v[k2] = sc[(k2 * GP + t) * STRIDE];
-    twiddle_mul<N, G, SIGN>(v, t, tab);
+    twiddle_mul<N, G, SIGN, TS>(v, t, tab);
     dft_reg<E, SIGN>(v);
 }
 

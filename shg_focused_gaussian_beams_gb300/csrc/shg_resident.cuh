@@ -56,7 +56,14 @@ __global__ void __launch_bounds__(ResShape<N, CS_, MINB_, G_>::THREADS, MINB_)
     extern __shared__ float2 smem[];
     float2 *sP = smem, *sS = smem + FIELD, *scr = smem + 2 * FIELD;
     __shared__ int job_s;
-    const float2 *__restrict__ tab = g_twiddle + N;
+    // this split's inter-stage twiddle pairs, staged in shared memory once per launch (the
+    // transforms then read them with shared loads instead of global ones)
+    __shared__ __align__(16) float2 tab[N];
+    {
+        const float2 *src = twiddle_split<N, G>(g_twiddle + N);
+        for (int i = threadIdx.x; i < N; i += blockDim.x) tab[i] = src[i];
+    }
+    __syncthreads();
     int rank = 0;
     if constexpr (CS > 1) rank = (int)cg::this_cluster().block_rank();
     const int tid = threadIdx.x;
@@ -108,8 +115,8 @@ __global__ void __launch_bounds__(ResShape<N, CS_, MINB_, G_>::THREADS, MINB_)
                     const float4 c = ccur;
 #pragma unroll
                     for (int j = 0; j < E; ++j) rk4_point(vp[j], vs[j], c, d);
-                    fft_nat_to_spec<N, G, +1>(vp, t, rsc, tab);
-                    fft_nat_to_spec<N, G, +1>(vs, t, rsc, tab);
+                    fft_nat_to_spec<N, G, +1, false, 1, G + 1, true>(vp, t, rsc, tab);
+                    fft_nat_to_spec<N, G, +1, false, 1, G + 1, true>(vs, t, rsc, tab);
                     __syncwarp();
 #pragma unroll
                     for (int r = 0; r < E; ++r) {
@@ -118,8 +125,8 @@ __global__ void __launch_bounds__(ResShape<N, CS_, MINB_, G_>::THREADS, MINB_)
                         rowS[k] = vs[r];
                     }
                 } else {
-                    fft_nat_to_spec<N, G, -1>(vp, t, rsc, tab);
-                    fft_nat_to_spec<N, G, -1>(vs, t, rsc, tab);
+                    fft_nat_to_spec<N, G, -1, false, 1, G + 1, true>(vp, t, rsc, tab);
+                    fft_nat_to_spec<N, G, -1, false, 1, G + 1, true>(vs, t, rsc, tab);
                     const float4 c1 = cprev;
 #pragma unroll
                     for (int r = 0; r < E; ++r) rk4_point(vp[r], vs[r], c1, d);
@@ -150,8 +157,8 @@ __global__ void __launch_bounds__(ResShape<N, CS_, MINB_, G_>::THREADS, MINB_)
                         const float4 c2 = ccur;
 #pragma unroll
                         for (int r = 0; r < E; ++r) rk4_point(vp[r], vs[r], c2, d);
-                        fft_spec_to_nat<N, G, +1>(vp, t, rsc, tab);
-                        fft_spec_to_nat<N, G, +1>(vs, t, rsc, tab);
+                        fft_spec_to_nat<N, G, +1, false, 1, G + 1, true>(vp, t, rsc, tab);
+                        fft_spec_to_nat<N, G, +1, false, 1, G + 1, true>(vs, t, rsc, tab);
 #pragma unroll
                         for (int j = 0; j < E; ++j) {
                             rowP[t + G * j] = vp[j];
@@ -188,10 +195,10 @@ __global__ void __launch_bounds__(ResShape<N, CS_, MINB_, G_>::THREADS, MINB_)
                     float2 v[E];
 #pragma unroll
                     for (int j = 0; j < E; ++j) v[j] = *at(j);
-                    fft_nat_to_spec<N, G, +1, true, R, G>(v, ct, scr + cc, tab);
+                    fft_nat_to_spec<N, G, +1, true, R, G, true>(v, ct, scr + cc, tab);
 #pragma unroll
                     for (int r = 0; r < E; ++r) v[r] = c_mul(v[r], h[r]);
-                    fft_spec_to_nat<N, G, -1, true, R, G>(v, ct, scr + cc, tab);
+                    fft_spec_to_nat<N, G, -1, true, R, G, true>(v, ct, scr + cc, tab);
 #pragma unroll
                     for (int j = 0; j < E; ++j) *at(j) = v[j];
                     __syncthreads();  // scratch reuse by the second field

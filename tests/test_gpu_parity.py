@@ -295,3 +295,27 @@ def test_cluster_march_matches_streaming(n, nzs):
         np.testing.assert_allclose(eta, eta_r, rtol=1e-12, atol=0)
     ref.close()
     sw.close()
+
+
+@pytest.mark.parametrize("nz", [2, 3])
+@pytest.mark.parametrize("n,schedules", [(64, ["streaming", "1/1", "8/8", "coop", "cluster"]),
+                                         (128, ["streaming", "2/1", "16/8", "coop", "cluster"]),
+                                         (256, ["streaming", "16/2", "coop", "cluster"])])
+def test_shortest_solves_on_every_schedule_vs_oracle(n, schedules, nz):
+    """The shortest marches the method allows (NZ = 2: one SSFM step; NZ = 3) on the streaming
+    passes, resident clusters, the persistent grid and the cluster march, against the oracle:
+    the first and last stage of a march coincide or touch, and no schedule may drop or repeat
+    one."""
+    inst = W.plain_instance(n, nz, 25.0, 2.84, 50.0)
+    po_r, so_r = O.Oracle(O.make_cfg(W.CRYSTAL_QPM50, n, n, nz, inst.lx, inst.ly)).run_plain(
+        inst.power, inst.waist, inst.focal, inst.temp)
+    for sched in schedules:
+        sw = Sweep([inst], crystal=W.CRYSTAL_QPM50)
+        if sched in ("streaming", "coop", "cluster"):
+            sw.set_schedule(n, resident=False if sched == "streaming" else sched)
+        else:
+            cs, mb = (int(v) for v in sched.split("/"))
+            sw.set_schedule(n, cluster_size=cs, ctas_per_sm=mb)
+        _, f = sw.run(with_fields=True)
+        sw.close()
+        assert rel_l2(f[0], so_r) < FIELD_RTOL, sched
