@@ -75,7 +75,13 @@ __global__ void __launch_bounds__(CptShape<N>::TPB, 1)
     constexpr int G = Sh::G, E = Sh::E, R = Sh::R, N2 = R * G, TC = Sh::TC, FIELD = Sh::FIELD;
     extern __shared__ float2 smem[];
     float2 *const sP = smem, *const sS = smem + FIELD, *const scr = smem + 2 * FIELD;
-    const float2 *__restrict__ tab = g_twiddle + N;
+    // the split's twiddle pairs, staged in shared memory once per launch
+    __shared__ __align__(16) float2 tab[N];
+    {
+        const float2 *src = twiddle_split<N, G>(g_twiddle + N);
+        for (int i = threadIdx.x; i < N; i += blockDim.x) tab[i] = src[i];
+    }
+    __syncthreads();
     cg::cluster_group cluster = cg::this_cluster();
     const int rank = (int)cluster.block_rank();
     const InstDesc &d = inst[list[blockIdx.x / Sh::CS]];
@@ -128,7 +134,7 @@ __global__ void __launch_bounds__(CptShape<N>::TPB, 1)
                 float2 v[E];
 #pragma unroll
                 for (int j = 0; j < E; ++j) v[j] = rline[rt + G * j];
-                fft_nat_to_spec<N, G, +1>(v, rt, rsc, tab);
+                fft_nat_to_spec<N, G, +1, false, 1, G + 1, true>(v, rt, rsc, tab);
 #pragma unroll
                 for (int r = 0; r < E; ++r) rline[spec_index<N, G>(rt, r)] = v[r];
             }
@@ -140,7 +146,7 @@ __global__ void __launch_bounds__(CptShape<N>::TPB, 1)
                 float2 v[E];
 #pragma unroll
                 for (int j = 0; j < E; ++j) v[j] = rline[rt + G * j];
-                fft_nat_to_spec<N, G, -1>(v, rt, rsc, tab);
+                fft_nat_to_spec<N, G, -1, false, 1, G + 1, true>(v, rt, rsc, tab);
 #pragma unroll
                 for (int r = 0; r < E; ++r) rline[spec_index<N, G>(rt, r)] = v[r];
             }
@@ -177,7 +183,7 @@ __global__ void __launch_bounds__(CptShape<N>::TPB, 1)
                 float2 v[E];
 #pragma unroll
                 for (int r = 0; r < E; ++r) v[r] = rline[spec_index<N, G>(rt, r)];
-                fft_spec_to_nat<N, G, +1>(v, rt, rsc, tab);
+                fft_spec_to_nat<N, G, +1, false, 1, G + 1, true>(v, rt, rsc, tab);
 #pragma unroll
                 for (int j = 0; j < E; ++j) rline[rt + G * j] = v[j];
             }
@@ -196,10 +202,10 @@ __global__ void __launch_bounds__(CptShape<N>::TPB, 1)
             float2 v[E];
 #pragma unroll
             for (int j = 0; j < E; ++j) v[j] = *col_at(ct + G * j);
-            fft_nat_to_spec<N, G, +1, false, TC, G>(v, ct, csc, tab);
+            fft_nat_to_spec<N, G, +1, false, TC, G, true>(v, ct, csc, tab);
 #pragma unroll
             for (int r = 0; r < E; ++r) v[r] = c_mul(v[r], h[r]);
-            fft_spec_to_nat<N, G, -1, false, TC, G>(v, ct, csc, tab);
+            fft_spec_to_nat<N, G, -1, false, TC, G, true>(v, ct, csc, tab);
 #pragma unroll
             for (int j = 0; j < E; ++j) *col_at(ct + G * j) = v[j];
         }

@@ -230,13 +230,14 @@ struct PtRowShape {
 
 // The row pass of k_rows_pt for lines [line0, line0 + LPB) of solve d at stage s, on a block
 // of PtRowShape<N>::TPB threads (shared by the streaming launch and the persistent grid).
-template <int N>
+// twiddles: the line length's global block g_twiddle + N, or with TS the split's own pair
+// table staged in shared memory by the caller.
+template <int N, bool TS = false>
 __device__ __forceinline__ void rows_pt_body(const InstDesc &d, int line0, int s, float2 *scratch, float2 *lines0,
-                                             float2 *lines1) {
+                                             float2 *lines1, const float2 *tab) {
     using Sh = PtRowShape<N>;
     constexpr int G = Sh::G, E = N / G, LPB = Sh::LPB, FT = Sh::FT;
     constexpr int SC = LineScratch<N, G>::SIZE;
-    const float2 *__restrict__ tab = g_twiddle + N;
     const int tid = threadIdx.x;
     // transform role
     const bool xf = tid < 2 * FT;
@@ -262,7 +263,7 @@ __device__ __forceinline__ void rows_pt_body(const InstDesc &d, int line0, int s
             float2 v[E];
 #pragma unroll
             for (int j = 0; j < E; ++j) v[j] = fline[t + G * j];
-            fft_nat_to_spec<N, G, +1>(v, t, fsc, tab);
+            fft_nat_to_spec<N, G, +1, false, 1, G + 1, TS>(v, t, fsc, tab);
 #pragma unroll
             for (int r = 0; r < E; ++r) F[fbase + spec_index<N, G>(t, r)] = v[r];
         }
@@ -272,7 +273,7 @@ __device__ __forceinline__ void rows_pt_body(const InstDesc &d, int line0, int s
         float2 v[E];
 #pragma unroll
         for (int j = 0; j < E; ++j) v[j] = F[fbase + t + G * j];
-        fft_nat_to_spec<N, G, -1>(v, t, fsc, tab);
+        fft_nat_to_spec<N, G, -1, false, 1, G + 1, TS>(v, t, fsc, tab);
 #pragma unroll
         for (int r = 0; r < E; ++r) fline[spec_index<N, G>(t, r)] = v[r];
     }
@@ -299,7 +300,7 @@ __device__ __forceinline__ void rows_pt_body(const InstDesc &d, int line0, int s
         float2 v[E];
 #pragma unroll
         for (int r = 0; r < E; ++r) v[r] = fline[spec_index<N, G>(t, r)];
-        fft_spec_to_nat<N, G, +1>(v, t, fsc, tab);
+        fft_spec_to_nat<N, G, +1, false, 1, G + 1, TS>(v, t, fsc, tab);
 #pragma unroll
         for (int j = 0; j < E; ++j) F[fbase + t + G * j] = v[j];
     }
@@ -312,7 +313,7 @@ __global__ void __launch_bounds__(PtRowShape<N>::TPB) k_rows_pt(const InstDesc *
     __shared__ float2 lines[2][Sh::LPB * N];  // [field][line * N + x], natural x order
     const InstDesc &d = inst[list[blockIdx.x / Sh::BPI]];
     if (!check_solve<N>(d, s)) return;  // whole block
-    rows_pt_body<N>(d, (blockIdx.x % Sh::BPI) * Sh::LPB, s, scratch, lines[0], lines[1]);
+    rows_pt_body<N>(d, (blockIdx.x % Sh::BPI) * Sh::LPB, s, scratch, lines[0], lines[1], g_twiddle + N);
 }
 
 // The column pass of k_cols for column x of field f (0 pump, 1 SH) of solve d, lane t of the
@@ -409,18 +410,17 @@ struct CoopShape {
 // cols_body with the column's propagator values already in registers.
 template <int N, int TC>
 __device__ __forceinline__ void cols_body_h(const InstDesc &d, int x, int f, int t, float2 *sc,
-                                            const float2 (&h)[N / LineShape<N>::G]) {
-    constexpr int G = LineShape<N>::G, E = N / G;
-    const float2 *__restrict__ tab = g_twiddle + N;
+                                            const float2 (&h)[N / LineShape<N>::G], const float2 *tab) {
+    constexpr int G = LineShape<N>::G, E = N / G;  // tab: the split's pair table in shared memory
     float2 *F = f == 0 ? d.P : d.S;
     constexpr size_t NN = (size_t)N * N;
     float2 v[E];
 #pragma unroll
     for (int j = 0; j < E; ++j) v[j] = SHG_AT(F, (size_t)(t + G * j) * N + x, NN, kChkCoop);
-    fft_nat_to_spec<N, G, +1, false, TC, G>(v, t, sc, tab);
+    fft_nat_to_spec<N, G, +1, false, TC, G, true>(v, t, sc, tab);
 #pragma unroll
     for (int r = 0; r < E; ++r) v[r] = c_mul(v[r], h[r]);
-    fft_spec_to_nat<N, G, -1, false, TC, G>(v, t, sc, tab);
+    fft_spec_to_nat<N, G, -1, false, TC, G, true>(v, t, sc, tab);
 #pragma unroll
     for (int j = 0; j < E; ++j) SHG_AT(F, (size_t)(t + G * j) * N + x, NN, kChkCoop) = v[j];
 }
@@ -438,10 +438,16 @@ __global__ void __launch_bounds__(CoopShape<N>::TPB) k_march_coop(const InstDesc
     constexpr int G = Sh::G;
     __shared__ float2 scratch[2 * Sh::LPB * LineScratch<N, G>::SIZE];
     __shared__ float2 lines[2][Sh::LPB * N];
+    __shared__ __align__(16) float2 tws[N];  // the split's twiddle pairs, staged once per launch
     extern __shared__ float2 cscr[];
     const InstDesc &d = inst[list[0]];
     // every block of the grid leaves together (before its first barrier) on a bad descriptor
     if (!check_solve<N>(d, 0)) return;
+    {
+        const float2 *src = twiddle_split<N, G>(g_twiddle + N);
+        for (int i = threadIdx.x; i < N; i += blockDim.x) tws[i] = src[i];
+    }
+    __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int K = d.nsteps;
     const int u = blockIdx.x + gridDim.x * warp;
@@ -452,13 +458,13 @@ __global__ void __launch_bounds__(CoopShape<N>::TPB) k_march_coop(const InstDesc
     unsigned target = 0;
     for (int s = 0; s <= K; ++s) {
         for (int r = blockIdx.x; r < C::ROW_UNITS; r += gridDim.x) {
-            rows_pt_body<N>(d, r * Sh::LPB, s, scratch, lines[0], lines[1]);
+            rows_pt_body<N, true>(d, r * Sh::LPB, s, scratch, lines[0], lines[1], tws);
             __syncthreads();  // the block's line buffers are reused by its next unit
         }
         if (s == K) break;
         target += gridDim.x;
         if (!grid_barrier(bar, target, err)) return;
-        if (colw) cols_body_h<N, C::TC>(d, x, f, t, cscr + (size_t)warp * C::TC * N + lane % C::TC, h);
+        if (colw) cols_body_h<N, C::TC>(d, x, f, t, cscr + (size_t)warp * C::TC * N + lane % C::TC, h, tws);
         target += gridDim.x;
         if (!grid_barrier(bar, target, err)) return;
     }
