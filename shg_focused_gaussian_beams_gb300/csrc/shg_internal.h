@@ -98,6 +98,10 @@ cudaError_t launch_sq_sums(const float *Tf, const float *Ti, size_t n, double *o
 cudaError_t launch_sellmeier_tables(const float *T, float *NP, float *NS, float *DK, size_t n, float lp, float ls,
                                     float two_pi, float inv_lambda, int crystal, cudaStream_t st);
 cudaError_t launch_rows_th(int n, const InstDesc *d, const ThermDesc &th, int s, cudaStream_t st);
+// The whole THERMAL march of one solve (stages 0..nz) as one cooperative launch with bounded
+// grid barriers (bar: a zeroed word; err: the solve's error word, or-ed with 2 when a barrier
+// wait gave up). d == nullptr only checks that the grid fits co-resident.
+cudaError_t launch_coop_th(int n, const InstDesc *d, const ThermDesc &th, unsigned *bar, int *err, cudaStream_t st);
 
 // One solve's run parameters (Solver::run arguments and the temperatures its set-up
 // calls read).

@@ -18,6 +18,7 @@
 #include <math.h>
 
 #include "shg_internal.h"
+#include "shg_coop.cuh"
 #include "shg_march.cuh"
 
 namespace shg {
@@ -358,72 +359,10 @@ __global__ void __launch_bounds__(TC * LineShape<N>::G) k_cols(const InstDesc *_
 // in one launch, separated by grid-wide barriers instead of kernel boundaries. A lone solve
 // otherwise pays two dependent launches per z-step.
 
-// Poll limit of a grid-barrier wait (about a second).
-constexpr long long kGridWaitLimit = 1ll << 22;
-
-__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned *p) {
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ __forceinline__ void red_release_gpu(unsigned *p, unsigned v) {
-    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
-// Grid-wide barrier of a cooperative launch on a monotonic arrival counter (zeroed before
-// the launch): barrier number e of the run completes once e * gridDim.x arrivals are in.
-// Thread 0 of each block arrives with a release add (ordering the block's writes, which the
-// block barrier made its own, before the arrival) and polls with acquire loads (ordering
-// the other blocks' writes before this block's later loads). No reset step: a waiter reads
-// one word. Every wait is bounded: on timeout *err is set and false is returned (the
-// caller leaves the kernel), and a wait also ends once another block has set *err.
-__device__ __forceinline__ bool grid_barrier(unsigned *count, unsigned target, int *err) {
-    __shared__ int ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        red_release_gpu(count, 1u);
-        int good = 1;
-        for (long long it = 0; ld_acquire_gpu(count) < target; ++it) {
-            if (it >= kGridWaitLimit || *(volatile int *)err) {
-                atomicExch(err, 1);
-                good = 0;
-                break;
-            }
-            if (it >= 64) __nanosleep(32);
-        }
-        ok = good;
-    }
-    __syncthreads();
-    return ok != 0;
-}
-
-template <int N>
-struct CoopShape {
-    static constexpr int G = LineShape<N>::G, E = N / G;
-    static constexpr int TPB = PtRowShape<N>::TPB;
-    static constexpr int TC = 32 / G;                    // columns per column group (one warp)
-    static constexpr int ROW_UNITS = PtRowShape<N>::BPI;  // groups of LPB lines
-    static constexpr int COL_UNITS = 2 * (N / TC);       // column groups of both fields
-    static_assert(TC * G == 32, "a column group is one warp");
-};
-
-// cols_body with the column's propagator values already in registers.
-template <int N, int TC>
-__device__ __forceinline__ void cols_body_h(const InstDesc &d, int x, int f, int t, float2 *sc,
-                                            const float2 (&h)[N / LineShape<N>::G], const float2 *tab) {
-    constexpr int G = LineShape<N>::G, E = N / G;  // tab: the split's pair table in shared memory
-    float2 *F = f == 0 ? d.P : d.S;
-    constexpr size_t NN = (size_t)N * N;
-    float2 v[E];
-#pragma unroll
-    for (int j = 0; j < E; ++j) v[j] = SHG_AT(F, (size_t)(t + G * j) * N + x, NN, kChkCoop);
-    fft_nat_to_spec<N, G, +1, false, TC, G, true>(v, t, sc, tab);
-#pragma unroll
-    for (int r = 0; r < E; ++r) v[r] = c_mul(v[r], h[r]);
-    fft_spec_to_nat<N, G, -1, false, TC, G, true>(v, t, sc, tab);
-#pragma unroll
-    for (int j = 0; j < E; ++j) SHG_AT(F, (size_t)(t + G * j) * N + x, NN, kChkCoop) = v[j];
-}
+// Grid barrier, CoopShape and cols_body_h: shg_coop.cuh.
+static_assert(CoopShape<64>::TPB == PtRowShape<64>::TPB && CoopShape<256>::ROW_UNITS == PtRowShape<256>::BPI &&
+                  CoopShape<16>::TPB == PtRowShape<16>::TPB,
+              "the persistent grid's row units are the row pass's blocks");
 
 // Grid of B blocks of TPB threads; block b runs row units b, b + B, ... and column groups
 // b + B w (warp w < col_warps), whose propagator values stay in registers for the whole run.

@@ -13,6 +13,7 @@
 #include <string>
 
 #include "shg_internal.h"
+#include "shg_coop.cuh"
 #include "shg_thermal.cuh"
 
 namespace shg {
@@ -519,17 +520,20 @@ struct ThRowShape {
     static_assert(FFT_THREADS % 32 == 0 && 2 * FFT_THREADS <= TPB, "transform threads fill whole warps");
 };
 
-template <int N>
-__global__ void __launch_bounds__(ThRowShape<N>::TPB) k_rows_th(const InstDesc *__restrict__ dd, const ThermDesc th, int s) {
+// The THERMAL row pass for lines [line0, line0 + LPB) at stage s on a block of
+// ThRowShape<N>::TPB threads (shared by the streaming launch and the persistent grid).
+// Twiddles: the global block g_twiddle + N, or with TS the split's pair table staged in
+// shared memory by the caller.
+template <int N, bool TS = false>
+__device__ __forceinline__ void rows_th_body(const InstDesc &d, const ThermDesc &th, int line0, int s,
+                                             float2 *scratch, float2 (*lines)[ThRowShape<N>::LPB * N],
+                                             const float2 *tab) {
     using Sh = ThRowShape<N>;
     constexpr int G = Sh::G, E = N / G, LPB = Sh::LPB, FT = Sh::FFT_THREADS;
     constexpr int SC = LineScratch<N, G>::SIZE;
-    __shared__ float2 scratch[2 * LPB * SC];
-    __shared__ float2 lines[2][LPB * N];  // [field][line * N + x], natural x order
-    const InstDesc &d = *dd;
     // stages 0..nz: the THERMAL march runs one stage past the last slice (heat source of slice nz-1)
-    if (!SHG_REQUIRE(d.n == N && s >= 0 && s <= th.nz && (int)blockIdx.x < Sh::BPI, kChkThermalRows, s)) return;
-    const float2 *__restrict__ tab = g_twiddle + N;
+    if (!SHG_REQUIRE(d.n == N && s >= 0 && s <= th.nz && line0 >= 0 && line0 + LPB <= N, kChkThermalRows, s))
+        return;  // block-uniform
     const size_t nxy = (size_t)N * N;
     const int tid = threadIdx.x;
     // transform role: field f, line fl, thread t of the line
@@ -538,10 +542,10 @@ __global__ void __launch_bounds__(ThRowShape<N>::TPB) k_rows_th(const InstDesc *
     float2 *const F = f == 0 ? d.P : d.S;
     float2 *const fline = lines[f & 1] + fl * N;
     float2 *const fsc = scratch + (size_t)((f & 1) * LPB + fl) * SC;
-    const size_t fbase = (size_t)(blockIdx.x * LPB + fl) * N;
+    const size_t fbase = (size_t)(line0 + fl) * N;
     // point role: line l, column x
     const int l = tid / N, x = tid % N;
-    const size_t i2 = (size_t)(blockIdx.x * LPB + l) * N + x;
+    const size_t i2 = (size_t)(line0 + l) * N + x;
     float2 *const pP = lines[0] + l * N + x, *const pS = lines[1] + l * N + x;
 
     if (s == 0) {
@@ -558,7 +562,7 @@ __global__ void __launch_bounds__(ThRowShape<N>::TPB) k_rows_th(const InstDesc *
             float2 v[E];
 #pragma unroll
             for (int j = 0; j < E; ++j) v[j] = fline[t + G * j];
-            fft_nat_to_spec<N, G, +1>(v, t, fsc, tab);
+            fft_nat_to_spec<N, G, +1, false, 1, G + 1, TS>(v, t, fsc, tab);
 #pragma unroll
             for (int r = 0; r < E; ++r) F[fbase + spec_index<N, G>(t, r)] = v[r];
         }
@@ -569,7 +573,7 @@ __global__ void __launch_bounds__(ThRowShape<N>::TPB) k_rows_th(const InstDesc *
         float2 v[E];
 #pragma unroll
         for (int j = 0; j < E; ++j) v[j] = F[fbase + t + G * j];
-        fft_nat_to_spec<N, G, -1>(v, t, fsc, tab);
+        fft_nat_to_spec<N, G, -1, false, 1, G + 1, TS>(v, t, fsc, tab);
 #pragma unroll
         for (int r = 0; r < E; ++r) fline[spec_index<N, G>(t, r)] = v[r];
     }
@@ -624,9 +628,63 @@ __global__ void __launch_bounds__(ThRowShape<N>::TPB) k_rows_th(const InstDesc *
         float2 v[E];
 #pragma unroll
         for (int r = 0; r < E; ++r) v[r] = fline[spec_index<N, G>(t, r)];
-        fft_spec_to_nat<N, G, +1>(v, t, fsc, tab);
+        fft_spec_to_nat<N, G, +1, false, 1, G + 1, TS>(v, t, fsc, tab);
 #pragma unroll
         for (int j = 0; j < E; ++j) F[fbase + t + G * j] = v[j];
+    }
+}
+
+template <int N>
+__global__ void __launch_bounds__(ThRowShape<N>::TPB) k_rows_th(const InstDesc *__restrict__ dd, const ThermDesc th, int s) {
+    using Sh = ThRowShape<N>;
+    __shared__ float2 scratch[2 * Sh::LPB * LineScratch<N, Sh::G>::SIZE];
+    __shared__ float2 lines[2][Sh::LPB * N];  // [field][line * N + x], natural x order
+    rows_th_body<N>(*dd, th, blockIdx.x * Sh::LPB, s, scratch, lines, g_twiddle + N);
+}
+
+// Persistent THERMAL march of one solve on a cooperative grid (stages 0..nz): the row pass
+// above and the plain column pass (cols_body_h, the same diffraction as k_cols) separated by
+// bounded grid-wide barriers instead of kernel boundaries. Block b runs row units b, b + B,
+// ... and column groups b + B w (warp w < col_warps), whose propagator values stay in
+// registers for the whole run. bar: zeroed arrival counter; err: the solve's error word, or-ed
+// with 2 when a barrier wait gave up.
+template <int N>
+__global__ void __launch_bounds__(ThRowShape<N>::TPB) k_march_coop_th(const InstDesc *__restrict__ dd,
+                                                                      const ThermDesc th, unsigned *bar, int *err,
+                                                                      int col_warps) {
+    using Sh = ThRowShape<N>;
+    using C = CoopShape<N>;
+    static_assert(C::TPB == Sh::TPB && C::ROW_UNITS == Sh::BPI, "row units are the row pass's blocks");
+    constexpr int G = Sh::G;
+    __shared__ float2 scratch[2 * Sh::LPB * LineScratch<N, G>::SIZE];
+    __shared__ float2 lines[2][Sh::LPB * N];
+    __shared__ __align__(16) float2 tws[N];  // the split's twiddle pairs, staged once per launch
+    extern __shared__ float2 cscr[];
+    const InstDesc &d = *dd;
+    if (!SHG_REQUIRE(d.n == N && th.nz >= 1, kChkThermalRows, d.n)) return;  // the whole grid alike
+    {
+        const float2 *src = twiddle_split<N, G>(g_twiddle + N);
+        for (int i = threadIdx.x; i < N; i += blockDim.x) tws[i] = src[i];
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int u = blockIdx.x + gridDim.x * warp;
+    const bool colw = warp < col_warps && u < C::COL_UNITS;
+    const int f = u / (N / C::TC), x = (u % (N / C::TC)) * C::TC + lane % C::TC, t = lane / C::TC;
+    float2 h[C::E];
+    if (colw) hprop_load<N>(f == 0 ? d.Hp : d.Hs, x, t, h);
+    unsigned target = 0;
+    for (int s = 0; s <= th.nz; ++s) {
+        for (int r = blockIdx.x; r < C::ROW_UNITS; r += gridDim.x) {
+            rows_th_body<N, true>(d, th, r * Sh::LPB, s, scratch, lines, tws);
+            __syncthreads();  // the block's line buffers are reused by its next unit
+        }
+        if (s == th.nz) break;
+        target += gridDim.x;
+        if (!grid_barrier(bar, target, err, 2)) return;
+        if (colw) cols_body_h<N, C::TC>(d, x, f, t, cscr + (size_t)warp * C::TC * N + lane % C::TC, h, tws);
+        target += gridDim.x;
+        if (!grid_barrier(bar, target, err, 2)) return;
     }
 }
 
@@ -754,6 +812,59 @@ template <int N>
 static cudaError_t launch_rows_th_t(const InstDesc *d, const ThermDesc &th, int s, cudaStream_t st) {
     k_rows_th<N><<<ThRowShape<N>::BPI, ThRowShape<N>::TPB, 0, st>>>(d, th, s);
     return cudaGetLastError();
+}
+
+template <int N>
+static cudaError_t launch_coop_th_t(const InstDesc *d, const ThermDesc &th, unsigned *bar, int *err, cudaStream_t st) {
+    using C = CoopShape<N>;
+    constexpr int warps = C::TPB / 32;
+    auto k = k_march_coop_th<N>;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaError_t e;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    // one column group per block where that many blocks fit co-resident, else the fewest
+    // blocks that hold every row unit (as for the plain persistent grid)
+    int blocks = 0, col_warps = 0;
+    size_t smem = 0;
+    for (int pass = 0; pass < 2 && !blocks; ++pass) {
+        int b = C::ROW_UNITS;
+        if (pass == 0 && C::COL_UNITS > b) b = C::COL_UNITS;
+        if ((C::COL_UNITS + warps - 1) / warps > b) b = (C::COL_UNITS + warps - 1) / warps;
+        const int cw = (C::COL_UNITS + b - 1) / b;
+        const size_t sm = (size_t)cw * C::TC * N * sizeof(float2);
+        if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) != cudaSuccess) return e;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, C::TPB, sm)) != cudaSuccess) return e;
+        if (per_sm * sms >= b) {
+            blocks = b;
+            col_warps = cw;
+            smem = sm;
+        }
+    }
+    if (!blocks) return cudaErrorCooperativeLaunchTooLarge;
+    if (!d) return cudaSuccess;  // fit check only
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(blocks, 1, 1);
+    cfg.blockDim = dim3(C::TPB, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, d, th, bar, err, col_warps);
+}
+
+cudaError_t launch_coop_th(int n, const InstDesc *d, const ThermDesc &th, unsigned *bar, int *err, cudaStream_t st) {
+    switch (n) {
+        case 16: return launch_coop_th_t<16>(d, th, bar, err, st);
+        case 32: return launch_coop_th_t<32>(d, th, bar, err, st);
+        case 64: return launch_coop_th_t<64>(d, th, bar, err, st);
+        case 128: return launch_coop_th_t<128>(d, th, bar, err, st);
+        case 256: return launch_coop_th_t<256>(d, th, bar, err, st);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 cudaError_t launch_rows_th(int n, const InstDesc *d, const ThermDesc &th, int s, cudaStream_t st) {

@@ -139,14 +139,17 @@ int ThermalSolve::create(const shg_config &cfg) {
     TH_CUDA(cudaMalloc(&dkint_, nn * sizeof(float)));
     TH_CUDA(cudaMalloc(&f_, 6 * nn * sizeof(float2)));
     TH_CUDA(cudaMalloc(&stepc_, (size_t)nz_ * sizeof(float4)));
-    // [0..3] power sums, [4] list entry, [5..6] residual sums, [7] the heat-sweep error word
-    // (an int, set by a TMA pipeline wait that gave up; read with the residual sums)
-    TH_CUDA(cudaMalloc(&acc_, 8 * sizeof(double)));
+    // [0..3] power sums, [4] list entry, [5..6] residual sums, [7] the error word (an int,
+    // or-ed with 1 by a TMA pipeline wait that gave up, with 2 by a grid-barrier wait of the
+    // persistent march that gave up; read with the residual sums), [8] the persistent march's
+    // arrival counter
+    TH_CUDA(cudaMalloc(&acc_, 9 * sizeof(double)));
     TH_CUDA(cudaMalloc(&d_desc_, sizeof(InstDesc)));
     TH_CUDA(cudaMemset(qk_, 0, tsize_ * sizeof(float)));
-    TH_CUDA(cudaMemset(acc_, 0, 8 * sizeof(double)));
+    TH_CUDA(cudaMemset(acc_, 0, 9 * sizeof(double)));
     scratch_sum_ = acc_ + 5;
     err_ = reinterpret_cast<int *>(acc_ + 7);
+    coop_bar_ = reinterpret_cast<unsigned *>(acc_ + 8);
     return SHG_OK;
 }
 
@@ -157,8 +160,21 @@ int ThermalSolve::check_error_word(const double *words) {
     if (!flag) return SHG_OK;
     TH_CUDA(cudaMemsetAsync(err_, 0, sizeof(int), st_));
     TH_CUDA(cudaStreamSynchronize(st_));
-    set_error("heat sweep: a TMA pipeline wait gave up (sweep incomplete)");
+    set_error((flag & 1) ? "heat sweep: a TMA pipeline wait gave up (sweep incomplete)"
+                         : "THERMAL march: a grid-barrier wait of the persistent launch gave up (march incomplete)");
     return SHG_ERR_CUDA;
+}
+
+// The THERMAL march as one persistent cooperative launch where its grid fits co-resident
+// (SHG_THERMAL_MARCH=streaming keeps the two launches per z-step), decided once.
+bool ThermalSolve::use_coop() {
+    if (coop_ < 0) {
+        const char *m = std::getenv("SHG_THERMAL_MARCH");
+        const bool want = !(m && std::string(m) == "streaming");
+        coop_ = want && launch_coop_th(n_, nullptr, th_, nullptr, nullptr, nullptr) == cudaSuccess ? 1 : 0;
+        cudaGetLastError();
+    }
+    return coop_ == 1;
 }
 
 int ThermalSolve::sq_diff(float *out) {
@@ -331,6 +347,11 @@ int ThermalSolve::cwes(float power, float waist, float focal) {
         TH_CUDA(cudaMemcpyAsync(slices_, h_desc_.P, nn * sizeof(float2), cudaMemcpyDeviceToDevice, st_));
         TH_CUDA(cudaMemcpyAsync(slices_ + nn, h_desc_.S, nn * sizeof(float2), cudaMemcpyDeviceToDevice, st_));
     }
+    if (use_coop()) {
+        TH_CUDA(cudaMemsetAsync(coop_bar_, 0, sizeof(unsigned), st_));
+        TH_CUDA(launch_coop_th(n_, d_desc_, th_, coop_bar_, err_, st_));
+        return SHG_OK;
+    }
     const int *list0 = reinterpret_cast<const int *>(acc_ + 4);
     for (int s = 0; s <= nz_; ++s) {
         TH_CUDA(launch_rows_th(n_, d_desc_, th_, s, st_));
@@ -357,7 +378,11 @@ int ThermalSolve::run(float power, float waist, float focal, float temp, float t
         if (counter == 1 && global_count != 0) global_count = num_of_iter;
         global_count++;
     }
+    // the error word once more: a persistent march that gave up in the last CWES
+    double w = 0.0;
+    TH_CUDA(cudaMemcpyAsync(&w, acc_ + 7, sizeof(double), cudaMemcpyDeviceToHost, st_));
     TH_CUDA(cudaStreamSynchronize(st_));
+    TH_TRY(check_error_word(&w));
     have_result_ = true;
     return SHG_OK;
 }

@@ -70,6 +70,7 @@ class ThermalSolve {
    private:
     int sq_diff(float *out);
     int check_error_word(const double *words);
+    bool use_coop();
     int jacobi_run(float t_inf, int *counter);
     shg_config cfg_{};
     int n_ = 0, nz_ = 0, bc_ = 0;
@@ -80,7 +81,9 @@ class ThermalSolve {
     float2 *f_ = nullptr;   // P, S, Pout, Sout, Hp, Hs
     float4 *stepc_ = nullptr;
     double *acc_ = nullptr, *scratch_sum_ = nullptr;
-    int *err_ = nullptr;  // heat-sweep error word of this solve (in acc_)
+    int *err_ = nullptr;  // error word of this solve (in acc_): 1 heat sweep, 2 persistent march
+    unsigned *coop_bar_ = nullptr;  // arrival counter of the persistent march (in acc_)
+    int coop_ = -1;                 // the THERMAL march as one persistent launch: -1 undecided
     InstDesc *d_desc_ = nullptr;
     InstDesc h_desc_{};
     ThermDesc th_{};

@@ -157,3 +157,24 @@ def test_relative_residual_stop_rule():
     assert cb != a.jacobi_counts()
     assert np.max(np.abs(b.temperature() - a.temperature())) < 0.25
     assert abs(b.efficiency() - a.efficiency()) / a.efficiency() < 0.1
+
+
+@pytest.mark.parametrize("n,nz,bc", [(64, 40, 1), (256, 24, 0), (32, 16, 1)])
+def test_persistent_thermal_march_matches_streaming(n, nz, bc, monkeypatch):
+    """The THERMAL march as one persistent cooperative launch (row and column passes between
+    bounded grid barriers) gives the two-launches-per-step march's fields, temperature and
+    Jacobi counts bit for bit, over a whole Solver::run (five outer iterations)."""
+    inst = W.plain_instance(n, nz, 25.0, 2.84, 51.0)
+    out = {}
+    for mode in ("streaming", "coop"):
+        monkeypatch.setenv("SHG_THERMAL_MARCH", mode)
+        s = S.Solver(crystal=W.CRYSTAL_QPM50, nx=n, ny=n, nz=nz, lx=inst.lx, ly=inst.ly, thermal=True, bc=bc)
+        s.run(25.0, inst.waist, FOCAL, 51.0, 25.0, 51.0, 51.0)
+        out[mode] = (s.fields(), s.temperature(), s.jacobi_counts(), s.efficiency())
+        s.close()
+    (fs, Ts, cs, es), (fc, Tc, cc, ec) = out["streaming"], out["coop"]
+    assert cs == cc
+    assert bits_equal(Ts, Tc)
+    for a, b in zip(fs, fc):
+        assert bits_equal(a, b)
+    assert abs(es - ec) <= 1e-12 * abs(es)
