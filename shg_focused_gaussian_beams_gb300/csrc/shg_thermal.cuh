@@ -183,11 +183,19 @@ __device__ __forceinline__ bool div_in_range(float a) {
     return m >= 0x1p-100f && m < 0x1p101f;
 }
 
+// All three in range at once: the smallest magnitude >= 2^-100 and the largest < 2^101
+// (a NaN may pass through fminf/fmaxf, but then both paths give NaN).
+__device__ __forceinline__ bool div_in_range3(float a, float b, float c) {
+    const float lo = fminf(fminf(fabsf(a), fabsf(b)), fabsf(c));
+    const float hi = fmaxf(fmaxf(fabsf(a), fabsf(b)), fabsf(c));
+    return lo >= 0x1p-100f && hi < 0x1p101f;
+}
+
 __device__ __forceinline__ float interior_voxel(const HeatCoef &c, float xm, float xp, float ym, float yp, float zm,
                                                 float zp, float qk) {
     const float sx = __fadd_rn(xp, xm), sy = __fadd_rn(yp, ym), sz = __fadd_rn(zp, zm);
     float a, b, d;
-    if (c.fast_div && div_in_range(sx) && div_in_range(sy) && div_in_range(sz)) {
+    if (c.fast_div && div_in_range3(sx, sy, sz)) {
         const float qa = sx * c.rdx2, qb = sy * c.rdy2, qd = sz * c.rdz2;
         a = fmaf(fmaf(-qa, c.dx2, sx), c.rdx2, qa);
         b = fmaf(fmaf(-qb, c.dy2, sy), c.rdy2, qb);
