@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(THREADS) k_heat_tma(float *__restrict__ Tf, co
             const float zm = sT[sm * TS + k], zp = sT[sp * TS + k];
             const float qk = sQ[s0 * QS + (warp + CONSUMER_WARPS * r) * TX + lane];
             if (in[r]) {
-                const long long vi = (long long)z * sxy + (long long)y * nx + x;
+                const int vi = z * sxy + y * nx + x;  // voxel count < 2^31 (checked on the host)
                 if (colint[r] && zint) {
                     SHG_AT(Tf, vi, (long long)sxy * nz, kChkHeatVoxel) =
                         interior_voxel(c, P[k - 1], P[k + 1], P[k - BX], P[k + BX], zm, zp, qk);
