@@ -127,16 +127,23 @@ static int enqueue_pass(const InstDesc &h, const InstDesc *d, AdjointWork &w, in
     const size_t nn = (size_t)n * n, st2 = 2 * nn;
     int rc;
     AD_CUDA(cudaMemsetAsync(w.acc_step, 0, sizeof(double) * (8 * (size_t)K + 3), st));
-    // forward from the inputs: checkpoints every L steps (store_all: X_s, W_s, F_s of every
-    // step); X_K into w.X
+    // Checkpointed: segment seg's X_s, W_s, F_s go to slot set seg & 1, replayed there from
+    // its checkpoint, or, for the last two segments, written by the forward pass itself
+    // (the two slot sets hold them; no replay). store_all: slot s of one set of K.
+    auto slot = [&](int s) -> size_t {
+        return store_all ? (size_t)s * st2 : (size_t)((s / L) & 1) * L * st2 + (size_t)(s % L) * st2;
+    };
+    auto stored = [&](int seg) -> bool { return store_all || seg >= nseg - 2; };
+    // forward from the inputs (X_K into w.X), keeping what the backward pass reads
     for (int s = 0; s <= K; ++s) {
         const bool fin = s > 0, start = s < K;
-        float2 *w_out = (store_all && fin) ? w.Ws + (size_t)(s - 1) * st2 : nullptr;
-        float2 *x_out = (store_all && start) ? w.Xs + (size_t)s * st2 : nullptr;
-        float2 *ck_out = (!store_all && start && s % L == 0) ? w.ck + (size_t)(s / L) * st2 : nullptr;
+        float2 *w_out = (fin && stored((s - 1) / L)) ? w.Ws + slot(s - 1) : nullptr;
+        float2 *x_out = (start && stored(s / L)) ? w.Xs + slot(s) : nullptr;
+        float2 *ck_out = (start && !stored(s / L) && s % L == 0) ? w.ck + (size_t)(s / L) * st2 : nullptr;
         AD_CUDA(launch_adj_rows_fwd(n, d, w.X, s, fin, start, h.P, h.S, w_out, x_out, ck_out, start ? nullptr : w.X,
                                     st));
-        if (start) AD_CUDA(launch_colpass(n, 0, w.X, store_all ? w.Fs + (size_t)s * st2 : nullptr, d, nullptr, st));
+        if (start)
+            AD_CUDA(launch_colpass(n, 0, w.X, stored(s / L) ? w.Fs + slot(s) : nullptr, d, nullptr, st));
     }
     AD_CUDA(launch_abs2_sum(w.X + nn, (int)nn, w.acc_glob + 2, st));
     AD_CUDA(launch_seed_cotangent(w.X + nn, w.cot, w.cot + nn, (int)nn, w.acc_glob + 3, st));
@@ -180,11 +187,10 @@ static int enqueue_pass(const InstDesc &h, const InstDesc *d, AdjointWork &w, in
         AD_CUDA(cudaStreamWaitEvent(b, w.ev, 0));
         return SHG_OK;
     };
-    if ((rc = join(st, w.side)) || (rc = replay(nseg - 1))) return rc;
     for (int seg = nseg - 1; seg >= 0; --seg) {
-        if ((rc = join(w.side, st))) return rc;  // replay(seg) done
+        if (!stored(seg) && (rc = join(w.side, st))) return rc;  // replay(seg) done
         // replay(seg-1) reuses the slot set of backward(seg+1), which st has finished
-        if (seg >= 1 && ((rc = join(st, w.side)) || (rc = replay(seg - 1)))) return rc;
+        if (seg >= 1 && !stored(seg - 1) && ((rc = join(st, w.side)) || (rc = replay(seg - 1)))) return rc;
         const int s0 = seg * L, s1 = std::min(K, s0 + L);
         if ((rc = backward(s0, s1, (size_t)(seg & 1) * L * st2))) return rc;
     }
@@ -213,8 +219,12 @@ int adjoint_run(const shg_config &cfg, const InstDesc &h, const InstDesc *d, flo
     if (!w.graph || std::memcmp(key, w.graph_key, sizeof(key)) != 0) {
         if (w.graph) cudaGraphExecDestroy(w.graph);
         w.graph = nullptr;
-        if (!w.cap) AD_CUDA(cudaStreamCreateWithFlags(&w.cap, cudaStreamNonBlocking));
-        if (!w.side) AD_CUDA(cudaStreamCreateWithFlags(&w.side, cudaStreamNonBlocking));
+        // the reverse sweep (captured on w.cap) is the pass's critical path: its nodes get the
+        // higher block-scheduling priority, the replay branch (w.side) the lower one
+        int prio_lo = 0, prio_hi = 0;
+        AD_CUDA(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
+        if (!w.cap) AD_CUDA(cudaStreamCreateWithPriority(&w.cap, cudaStreamNonBlocking, prio_hi));
+        if (!w.side) AD_CUDA(cudaStreamCreateWithPriority(&w.side, cudaStreamNonBlocking, prio_lo));
         if (!w.ev) AD_CUDA(cudaEventCreateWithFlags(&w.ev, cudaEventDisableTiming));
         cudaGraph_t g = nullptr;
         AD_CUDA(cudaStreamBeginCapture(w.cap, cudaStreamCaptureModeThreadLocal));
@@ -225,7 +235,7 @@ int adjoint_run(const shg_config &cfg, const InstDesc &h, const InstDesc *d, flo
             return rc;
         }
         AD_CUDA(e);
-        e = cudaGraphInstantiate(&w.graph, g, 0);
+        e = cudaGraphInstantiate(&w.graph, g, cudaGraphInstantiateFlagUseNodePriority);
         cudaGraphDestroy(g);
         AD_CUDA(e);
         std::memcpy(w.graph_key, key, sizeof(key));
