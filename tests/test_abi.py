@@ -57,3 +57,15 @@ def test_python_sellmeier_matches_oracle():
     for T in np.linspace(10, 90, 41, dtype=np.float32):
         for L in (1.064, np.float32(0.532), 0.8):
             assert sellmeier_n(L, T) == O.lib().oracle_n_f32(L, T)
+
+
+def test_check_status_of_a_build_without_checks():
+    """The normal library reports that it carries no device-side checks, without a GPU."""
+    import ctypes as C
+    from shg_focused_gaussian_beams_gb300 import _lib
+    L = _lib.lib()
+    e, s, v = C.c_int(-1), C.c_int(-1), C.c_longlong(-1)
+    assert L.shg_check_status(C.byref(e), C.byref(s), C.byref(v)) == 0
+    assert (e.value, s.value, v.value) == (0, 0, 0)
+    assert L.shg_check_status(None, C.byref(s), C.byref(v)) == 1
+    assert L.shg_check_selftest(7) == 2 and b"SHG_CHECK" in L.shg_last_error()
