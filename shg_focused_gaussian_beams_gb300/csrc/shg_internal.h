@@ -32,7 +32,7 @@ unsigned long long check_word_take_heat_tma();
 unsigned long long check_word_take_adjoint();
 cudaError_t launch_check_selftest(long long value);
 
-// shg_march_v1.cu (resident march): variants (cluster size, CTAs per SM) per grid size
+// shg_resident_variants.cu (resident march): variants (cluster size, CTAs per SM) per grid size
 struct ResidentVariant {
     int cs, minb, g;  // cluster size, CTAs per SM, threads per line (FFT split N = (N/g) x g);
                       // cs == 0: the persistent cooperative grid of one solve (launch_coop);

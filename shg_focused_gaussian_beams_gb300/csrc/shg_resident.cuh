@@ -1,4 +1,4 @@
-// Resident z-march kernel template (see shg_march_v1.cu); instantiated per grid size in
+// Resident z-march kernel template (design notes in shg_resident_variants.cu); instantiated per grid size in
 // shg_resident_<n>.cu.
 #pragma once
 
