@@ -15,6 +15,8 @@ batch with its schedules, the heat components, argument errors.
 mode "host": the sanitizer build's paths that need no GPU (crystal indices, argument
 errors), for the CPU test suite.
 
+mode "fullsize": the SHG_CHECK build on the benchmarked workloads at their own sizes.
+
 Prints one JSON line; exit status 0 when every comparison held.
 """
 from __future__ import annotations
@@ -161,6 +163,29 @@ def error_cases():
     record("null_config", rc == 1)
 
 
+def fullsize_cases():
+    """The benchmarked workloads at their own sizes: the 512-solve sweep (its autotuner runs
+    every candidate schedule of every class once), lone solves on the persistent grid at
+    128x128x200 and 256x256x400, and a THERMAL 256x256x400 run (persistent THERMAL march,
+    TMA heat sweeps, 1e-6 relative-residual rule)."""
+    from shg_focused_gaussian_beams_gb300.parallel import rank_sweep
+    sw = S.Sweep(rank_sweep(512, 2024, 0, 1, "weak"), crystal=CR)
+    eta = sw.run()
+    sw.close()
+    record("sweep512", bool(np.all(np.isfinite(eta))))
+    for n, nz in ((128, 200), (256, 400)):
+        lone = S.Sweep([W.plain_instance(n, nz, 10.0, 2.84, 50.0)], crystal=CR)
+        lone.set_schedule(n, resident="coop")
+        record(f"coop{n}x{nz}", bool(np.isfinite(lone.run()[0])))
+        lone.close()
+    inst = W.config_thermal_256()
+    s = S.Solver(crystal=CR, nx=inst.nx, ny=inst.ny, nz=inst.nz, lx=inst.lx, ly=inst.ly, thermal=True, bc=inst.bc)
+    s.set_jacobi_rule(1e-6, 100, 1000)
+    s.run(inst.power, inst.waist, inst.focal, inst.temp, inst.t_inf, inst.t1, inst.t2)
+    record("thermal256x400", np.isfinite(s.efficiency()), counts=s.jacobi_counts())
+    s.close()
+
+
 def host_cases():
     """Host-only paths (no GPU needed): crystal indices bit-equal to the oracle's, argument
     errors, and the check-status call of a build without checks."""
@@ -182,6 +207,12 @@ def host_cases():
 
 if MODE == "host":
     host_cases()
+    print(json.dumps(report))
+    sys.exit(0 if ok else 1)
+if MODE == "fullsize":
+    fullsize_cases()
+    en, site, val = status()
+    record("no_failed_check", en == 1 and site == 0, site=site, value=val)
     print(json.dumps(report))
     sys.exit(0 if ok else 1)
 if MODE == "check":

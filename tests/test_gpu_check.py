@@ -47,3 +47,13 @@ def test_host_code_clean_under_asan_ubsan_on_gpu_paths(diag_libs):
     assert report is not None, err[-3000:]
     bad = {k: v for k, v in report["cases"].items() if not v["ok"]}
     assert rc == 0 and not bad, (bad, err[-2000:])
+
+
+def test_check_build_at_the_benchmarked_sizes(diag_libs):
+    """The SHG_CHECK build on the workloads as benchmarked: the 512-solve sweep with every
+    schedule the autotuner tries, lone 128x128x200 and 256x256x400 solves on the persistent
+    grid, and a THERMAL 256x256x400 run; no check may fail."""
+    rc, report, err = run_child("fullsize", diag_libs["check"], sanitize=False)
+    assert report is not None, err[-3000:]
+    bad = {k: v for k, v in report["cases"].items() if not v["ok"]}
+    assert rc == 0 and not bad, (bad, err[-2000:])
