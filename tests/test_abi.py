@@ -69,3 +69,47 @@ def test_check_status_of_a_build_without_checks():
     assert (e.value, s.value, v.value) == (0, 0, 0)
     assert L.shg_check_status(None, C.byref(s), C.byref(v)) == 1
     assert L.shg_check_selftest(7) == 2 and b"SHG_CHECK" in L.shg_last_error()
+
+
+def _header_struct_fields(name):
+    """Field names of `typedef struct <name> {...}` in include/shg.h, in declaration order."""
+    src = open(os.path.join(ROOT, "include", "shg.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    body = re.search(r"typedef struct %s \{(.*?)\}" % name, src, flags=re.S).group(1)
+    out = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        names = decl.split(None, 1)[1]  # drop the type
+        out += [re.sub(r"\[.*\]", "", n).strip() for n in names.split(",")]
+    return out
+
+
+@pytest.mark.parametrize("cname,pyname", [("shg_config", "Config"), ("shg_instance", "Instance"),
+                                          ("shg_kernel_stat", "KernelStat")])
+def test_python_structs_match_the_header_layout(cname, pyname, tmp_path):
+    """The ctypes structures of the binding have the header's fields, offsets and size (the
+    offsets as the C compiler lays them out), so shg_config_init and the batch calls write
+    exactly the Python objects' memory."""
+    import ctypes as C
+    import shutil
+    import subprocess
+    from shg_focused_gaussian_beams_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    fields = _header_struct_fields(cname)
+    py = getattr(_lib, pyname)
+    assert [f[0] for f in py._fields_] == fields
+    prog = ["#include <stddef.h>", "#include <stdio.h>", '#include "shg.h"', "int main(void) {",
+            '  printf("%%zu\\n", sizeof(%s));' % cname]
+    prog += ['  printf("%%zu\\n", offsetof(%s, %s));' % (cname, f) for f in fields]
+    prog += ["  return 0;", "}"]
+    c_src = tmp_path / "layout.c"
+    c_src.write_text("\n".join(prog) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(c_src), "-o", str(exe)], check=True)
+    vals = [int(v) for v in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    assert vals[0] == C.sizeof(py)
+    assert vals[1:] == [getattr(py, f).offset for f in fields]
