@@ -113,3 +113,58 @@ def test_python_structs_match_the_header_layout(cname, pyname, tmp_path):
     vals = [int(v) for v in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
     assert vals[0] == C.sizeof(py)
     assert vals[1:] == [getattr(py, f).offset for f in fields]
+
+
+def _prototypes():
+    """{name: (return type, [parameter types])} of every prototype in include/shg.h."""
+    src = open(os.path.join(ROOT, "include", "shg.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    out = {}
+    for ret, name, params in re.findall(r"^\s*((?:const\s+)?\w+(?:\s+\w+)?\s*\**)\s*(shg_\w+)\s*\(([^)]*)\)\s*;",
+                                        src, flags=re.M):
+        types = []
+        for p in params.split(","):
+            p = " ".join(p.split())
+            if p in ("", "void"):
+                continue
+            types.append(re.sub(r"\s*\b\w+$", "", p))  # drop the parameter's name
+        out[name] = (ret.strip(), types)
+    return out
+
+
+def test_binding_signatures_match_the_header_prototypes():
+    """Every argtypes / restype of the ctypes binding agrees with the C prototype: the same
+    number of arguments, the exact type of every scalar, and a pointer of the right kind for
+    every pointer (a wrong count or width would corrupt the call silently)."""
+    import ctypes as C
+    from shg_focused_gaussian_beams_gb300 import _lib
+    scalars = {"int": C.c_int, "float": C.c_float, "double": C.c_double, "long long": C.c_longlong}
+    structs = {"shg_config": _lib.Config, "shg_instance": _lib.Instance, "shg_kernel_stat": _lib.KernelStat}
+    opaque = {"void", "shg_handle", "shg_batch", "shg_thgrad"}
+
+    def ok(ctype, bound):
+        stars = ctype.count("*")
+        base = " ".join(ctype.replace("const", " ").replace("*", " ").split())
+        if stars == 0:
+            return bound is scalars.get(base, object())
+        if stars == 2:
+            return bound is C.POINTER(C.c_void_p)
+        if base == "char":
+            return bound is C.c_char_p
+        if base in scalars:
+            return bound in (C.POINTER(scalars[base]), C.c_void_p)
+        if base in structs:
+            return bound is C.POINTER(structs[base])
+        return base in opaque and bound is C.c_void_p
+
+    protos = _prototypes()
+    assert set(protos) == set(_declared())
+    bad = []
+    for name, (ret, params) in protos.items():
+        res, args = _lib.SIGNATURES[name]
+        want_res = {"int": C.c_int, "void": None, "double": C.c_double, "const char *": C.c_char_p}[ret]
+        if res is not want_res or len(args) != len(params):
+            bad.append((name, ret, params))
+            continue
+        bad += [(name, i, p) for i, (p, a) in enumerate(zip(params, args)) if not ok(p, a)]
+    assert not bad, bad
