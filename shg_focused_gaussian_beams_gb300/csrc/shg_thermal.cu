@@ -9,6 +9,7 @@
 // so delta-k(T) is bit-identical too.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdlib>
 #include <string>
 
@@ -700,14 +701,14 @@ cudaError_t launch_init_temperature(float *T, int nx, int ny, int nz, float temp
 template <int BC, int K>
 static cudaError_t launch_heat_tb_t(float *Tf, const float *Ti, const float *QK, const HeatCoef &c, int nx, int ny,
                                     int nz, cudaStream_t st) {
-    static unsigned long long done = 0;  // devices whose shared-memory limit is raised
+    static std::atomic<unsigned long long> done{0};  // devices whose shared-memory limit is raised
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    if (dev < 64 && !(done >> dev & 1ull)) {
+    if (dev >= 64 || !(done.load() >> dev & 1ull)) {
         e = cudaFuncSetAttribute(k_heat_tb<BC, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)HeatTB<K>::SMEM);
         if (e != cudaSuccess) return e;
-        done |= 1ull << dev;
+        if (dev < 64) done.fetch_or(1ull << dev);
     }
     dim3 grd((nx + TB_X - 1) / TB_X, (ny + TB_Y - 1) / TB_Y, (nz + TB_ZC - 1) / TB_ZC);
     k_heat_tb<BC, K><<<grd, HeatTB<K>::RP, HeatTB<K>::SMEM, st>>>(Tf, Ti, QK, c, nx, ny, nz);
