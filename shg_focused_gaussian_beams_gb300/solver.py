@@ -36,6 +36,21 @@ def _pf(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_float))
 
 
+def _device_field(t, numel, what):
+    """`t` if it is a contiguous complex64 CUDA tensor of `numel` elements, else ValueError:
+    the C ABI reads or writes exactly that many elements through the raw pointer."""
+    import torch
+    if (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.complex64 and t.is_contiguous()
+            and t.numel() == numel):
+        return t
+    if isinstance(t, torch.Tensor):
+        got = (f"a {t.dtype} {t.device.type} tensor of shape {tuple(t.shape)}"
+               + ("" if t.is_contiguous() else ", not contiguous"))
+    else:
+        got = type(t).__name__
+    raise ValueError(f"{what}: expected a contiguous complex64 CUDA tensor of {numel} elements, got {got}")
+
+
 class Solver:
     """One solve on the device (Solver.h:120-153)."""
 
@@ -99,10 +114,12 @@ class Solver:
     def cwes_device(self, temp, pump_in, sh_in=None, pump_out=None, sh_out=None, stream=None):
         """Device-pointer CWES on torch tensors (complex64, (NY, NX), contiguous)."""
         import torch
-        if pump_out is None:
-            pump_out = torch.empty_like(pump_in)
-        if sh_out is None:
-            sh_out = torch.empty_like(pump_in)
+        n = self.nx * self.ny
+        _device_field(pump_in, n, "pump_in")
+        if sh_in is not None:
+            _device_field(sh_in, n, "sh_in")
+        pump_out = torch.empty_like(pump_in) if pump_out is None else _device_field(pump_out, n, "pump_out")
+        sh_out = torch.empty_like(pump_in) if sh_out is None else _device_field(sh_out, n, "sh_out")
         st = torch.cuda.current_stream(pump_in.device).cuda_stream if stream is None else stream
         check(lib().shg_cwes_device(self._h, temp, pump_in.data_ptr(),
                                     None if sh_in is None else sh_in.data_ptr(), pump_out.data_ptr(),
@@ -118,6 +135,9 @@ class Solver:
         fields (torch complex64 CUDA tensors, dL/dRe + i dL/dIm), the oven temperature
         (fields held fixed) and the poling period. Returns a dict."""
         import torch
+        _device_field(pump_in, self.nx * self.ny, "pump_in")
+        if sh_in is not None:
+            _device_field(sh_in, self.nx * self.ny, "sh_in")
         gp = torch.empty_like(pump_in)
         gs = torch.empty_like(pump_in)
         out = (C.c_double * 4)()
@@ -137,9 +157,11 @@ class Solver:
         gp = torch.empty((self.ny, self.nx), dtype=torch.complex64, device=dev)
         out = (C.c_double * 8)()
         st = torch.cuda.current_stream(dev).cuda_stream if stream is None else stream
-        fac = None if pump_factor is None else pump_factor.contiguous().data_ptr()
-        check(lib().shg_grad_run(self._h, power, waist, focalpoint, temp, fac, int(checkpoints), gp.data_ptr(), out,
-                                 st), "shg_grad_run")
+        # the factor's contiguous copy, if one is made, stays referenced through the call
+        fac = None if pump_factor is None else _device_field(pump_factor.contiguous(), self.nx * self.ny,
+                                                            "pump_factor")
+        check(lib().shg_grad_run(self._h, power, waist, focalpoint, temp, None if fac is None else fac.data_ptr(),
+                                 int(checkpoints), gp.data_ptr(), out, st), "shg_grad_run")
         return {"loss": out[0], "grad_pump": gp, "dT": out[1], "dLambda": out[2], "ddk": out[3], "dfocal": out[4],
                 "dwaist": out[5], "dpower": out[6], "dT_total": out[7]}
 
@@ -356,7 +378,9 @@ class ThermalGradBatch:
 
     def set_temperature(self, i, T: np.ndarray, power, waist, focal):
         Tn = np.ascontiguousarray(T, np.float32)
-        assert Tn.size == self.nx * self.ny * self.nz
+        if Tn.size != self.nx * self.ny * self.nz:
+            raise ValueError(f"temperature field of {Tn.size} values, expected NX*NY*NZ = "
+                             f"{self.nx * self.ny * self.nz}")
         check(lib().shg_thgrad_set_temperature(self._h, int(i), _pf(Tn), power, waist, focal),
               "shg_thgrad_set_temperature")
 
@@ -376,10 +400,8 @@ class ThermalGradBatch:
               "shg_thgrad_gaussian_pumps")
         return out
 
-    def _check_pump(self, pump):
-        import torch
-        assert pump.dtype == torch.complex64 and pump.is_cuda and pump.is_contiguous()
-        assert tuple(pump.shape) == (self.count, self.ny, self.nx)
+    def _check_pump(self, pump, what="pump"):
+        _device_field(pump, self.count * self.ny * self.nx, what)
 
     def forward(self, pump, with_fields=False, stream=None):
         """Returns dict(p_sh, p_in [W] as numpy arrays, and with_fields: pump_out, sh_out)."""
@@ -402,6 +424,8 @@ class ThermalGradBatch:
         """Returns dict(p_sh, p_in, grad) with grad[i] = dP_SH,i / dA_in,i (dL/dRe + i dL/dIm)."""
         import torch
         self._check_pump(pump)
+        if grad is not None:
+            self._check_pump(grad, "grad")
         g = torch.empty_like(pump) if grad is None else grad
         psh = np.zeros(self.count)
         pin = np.zeros(self.count)
@@ -438,6 +462,8 @@ def init_temperature(crystal, nx, ny, nz, temp, t1, t2, bc, lx=None, ly=None):
 def heat_sweeps(crystal, T, Q, t_inf, nsweeps, bc, lx=None, ly=None):
     """`nsweeps` Jacobi sweeps of Tfield.h:113 (bc 0) / 224 (bc 1) on the device."""
     nz, ny, nx = T.shape
+    if np.shape(Q) != T.shape:
+        raise ValueError(f"heat source of shape {np.shape(Q)}, expected the temperature's {T.shape}")
     cfg = _grid_cfg(crystal, nx, ny, nz, lx, ly)
     Tn = np.ascontiguousarray(T, np.float32).copy()
     Qn = np.ascontiguousarray(Q, np.float32)
@@ -458,8 +484,11 @@ def dk_thermal(crystal, T, lx=None, ly=None):
 def dft2d_device(x, sign: int, out=None, stream=None):
     """Unnormalised 2D DFT of a square (n, n) complex64 CUDA tensor (FFTW sign convention)."""
     import torch
-    if out is None:
-        out = torch.empty_like(x)
+    if x.dim() != 2 or x.shape[0] != x.shape[1]:
+        raise ValueError(f"expected a square (n, n) tensor, got shape {tuple(x.shape)}")
+    n = int(x.shape[0])
+    _device_field(x, n * n, "x")
+    out = torch.empty_like(x) if out is None else _device_field(out, n * n, "out")
     st = torch.cuda.current_stream(x.device).cuda_stream if stream is None else stream
-    check(lib().shg_dft2d_device(x.shape[0], sign, x.data_ptr(), out.data_ptr(), st), "shg_dft2d_device")
+    check(lib().shg_dft2d_device(n, sign, x.data_ptr(), out.data_ptr(), st), "shg_dft2d_device")
     return out
