@@ -36,12 +36,15 @@ def _pf(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_float))
 
 
-def _device_field(t, numel, what):
-    """`t` if it is a contiguous complex64 CUDA tensor of `numel` elements, else ValueError:
-    the C ABI reads or writes exactly that many elements through the raw pointer."""
+def _device_field(t, numel, what, device=None):
+    """`t` if it is a contiguous complex64 CUDA tensor of `numel` elements (on CUDA device
+    `device` when given: the handle's), else ValueError: the C ABI reads or writes exactly
+    that many elements through the raw pointer, on the handle's device."""
     import torch
     if (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.complex64 and t.is_contiguous()
             and t.numel() == numel):
+        if device is not None and t.device.index != device:
+            raise ValueError(f"{what}: tensor on cuda:{t.device.index}, the handle's device is cuda:{device}")
         return t
     if isinstance(t, torch.Tensor):
         got = (f"a {t.dtype} {t.device.type} tensor of shape {tuple(t.shape)}"
@@ -114,12 +117,12 @@ class Solver:
     def cwes_device(self, temp, pump_in, sh_in=None, pump_out=None, sh_out=None, stream=None):
         """Device-pointer CWES on torch tensors (complex64, (NY, NX), contiguous)."""
         import torch
-        n = self.nx * self.ny
-        _device_field(pump_in, n, "pump_in")
+        n, dv = self.nx * self.ny, self.cfg.device
+        _device_field(pump_in, n, "pump_in", dv)
         if sh_in is not None:
-            _device_field(sh_in, n, "sh_in")
-        pump_out = torch.empty_like(pump_in) if pump_out is None else _device_field(pump_out, n, "pump_out")
-        sh_out = torch.empty_like(pump_in) if sh_out is None else _device_field(sh_out, n, "sh_out")
+            _device_field(sh_in, n, "sh_in", dv)
+        pump_out = torch.empty_like(pump_in) if pump_out is None else _device_field(pump_out, n, "pump_out", dv)
+        sh_out = torch.empty_like(pump_in) if sh_out is None else _device_field(sh_out, n, "sh_out", dv)
         st = torch.cuda.current_stream(pump_in.device).cuda_stream if stream is None else stream
         check(lib().shg_cwes_device(self._h, temp, pump_in.data_ptr(),
                                     None if sh_in is None else sh_in.data_ptr(), pump_out.data_ptr(),
@@ -135,9 +138,9 @@ class Solver:
         fields (torch complex64 CUDA tensors, dL/dRe + i dL/dIm), the oven temperature
         (fields held fixed) and the poling period. Returns a dict."""
         import torch
-        _device_field(pump_in, self.nx * self.ny, "pump_in")
+        _device_field(pump_in, self.nx * self.ny, "pump_in", self.cfg.device)
         if sh_in is not None:
-            _device_field(sh_in, self.nx * self.ny, "sh_in")
+            _device_field(sh_in, self.nx * self.ny, "sh_in", self.cfg.device)
         gp = torch.empty_like(pump_in)
         gs = torch.empty_like(pump_in)
         out = (C.c_double * 4)()
@@ -159,7 +162,7 @@ class Solver:
         st = torch.cuda.current_stream(dev).cuda_stream if stream is None else stream
         # the factor's contiguous copy, if one is made, stays referenced through the call
         fac = None if pump_factor is None else _device_field(pump_factor.contiguous(), self.nx * self.ny,
-                                                            "pump_factor")
+                                                            "pump_factor", self.cfg.device)
         check(lib().shg_grad_run(self._h, power, waist, focalpoint, temp, None if fac is None else fac.data_ptr(),
                                  int(checkpoints), gp.data_ptr(), out, st), "shg_grad_run")
         return {"loss": out[0], "grad_pump": gp, "dT": out[1], "dLambda": out[2], "ddk": out[3], "dfocal": out[4],
@@ -401,7 +404,7 @@ class ThermalGradBatch:
         return out
 
     def _check_pump(self, pump, what="pump"):
-        _device_field(pump, self.count * self.ny * self.nx, what)
+        _device_field(pump, self.count * self.ny * self.nx, what, self.device)
 
     def forward(self, pump, with_fields=False, stream=None):
         """Returns dict(p_sh, p_in [W] as numpy arrays, and with_fields: pump_out, sh_out)."""

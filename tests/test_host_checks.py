@@ -31,7 +31,7 @@ def test_dft2d_refuses_a_non_square_array_before_any_device_call():
 
 
 def test_batched_thermal_pumps_must_cover_every_solve():
-    fake = types.SimpleNamespace(count=3, ny=8, nx=8)
+    fake = types.SimpleNamespace(count=3, ny=8, nx=8, device=0)
     with pytest.raises(ValueError, match="pump: .*192 elements"):
         S.ThermalGradBatch._check_pump(fake, torch.zeros(2, 8, 8, dtype=torch.complex64))
     with pytest.raises(ValueError, match="grad: "):
