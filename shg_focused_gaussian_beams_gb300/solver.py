@@ -107,6 +107,9 @@ class Solver:
     def set_input_fields(self, pump: np.ndarray, sh: np.ndarray | None = None):
         p = np.ascontiguousarray(pump, np.complex64)
         s = None if sh is None else np.ascontiguousarray(sh, np.complex64)
+        for name, a in (("pump", p), ("sh", s)):
+            if a is not None and a.size != self.nx * self.ny:
+                raise ValueError(f"{name}: {a.size} points, expected NX*NY = {self.nx * self.ny}")
         check(lib().shg_set_input_fields(self._h, _pf(p), None if s is None else _pf(s)), "shg_set_input_fields")
 
     # Solver::CWES (Solver.h:245), plain
@@ -242,9 +245,20 @@ class Sweep:
     def run(self, with_fields=False, eta_out=None, sh_out_all=None):
         """Run every solve. Returns efficiencies, and the SH output fields (list of (n, n)
         complex64 views into one contiguous buffer) when with_fields is set.
-        eta_out / sh_out_all may be caller-owned (e.g. pinned) host buffers."""
+        eta_out / sh_out_all may be caller-owned (e.g. pinned) host buffers: eta_out a
+        contiguous float64 array of one value per solve, sh_out_all a contiguous complex64
+        array of every solve's points or the integer address of such a buffer."""
         eta = np.zeros(self.n, np.float64) if eta_out is None else eta_out
+        if not (isinstance(eta, np.ndarray) and eta.dtype == np.float64 and eta.flags.c_contiguous
+                and eta.size == self.n):
+            raise ValueError(f"eta_out: expected a contiguous float64 array of {self.n} values")
         buf = sh_out_all
+        if isinstance(buf, np.ndarray):
+            total = int(self.field_offsets()[-1])
+            if not (buf.dtype == np.complex64 and buf.flags.c_contiguous and buf.size == total):
+                raise ValueError(f"sh_out_all: expected a contiguous complex64 array of {total} points")
+        elif buf is not None and with_fields:
+            raise ValueError("with_fields needs sh_out_all as an array (or None), not an address")
         if with_fields and buf is None:
             buf = np.zeros(int(self.field_offsets()[-1]), np.complex64)
         ptr = None if buf is None else C.c_void_p(buf.ctypes.data if isinstance(buf, np.ndarray) else buf)

@@ -42,3 +42,23 @@ def test_heat_source_must_match_the_temperature_grid():
     T = np.zeros((4, 8, 8), np.float32)
     with pytest.raises(ValueError, match="heat source of shape"):
         S.heat_sweeps(None, T, np.zeros((4, 8, 9), np.float32), 25.0, 1, 0)
+
+
+def test_host_buffers_of_a_sweep_and_a_solve_are_checked():
+    """Sweep.run's caller-owned buffers and Solver.set_input_fields's arrays must hold
+    exactly what the C call copies (checked before the call; the objects here are stand-ins
+    with the attributes the methods read, so no device is needed)."""
+    sweep = types.SimpleNamespace(n=3, field_offsets=lambda: np.array([0, 4, 8, 12]))
+    with pytest.raises(ValueError, match="eta_out"):
+        S.Sweep.run(sweep, eta_out=np.zeros(3, np.float32))
+    with pytest.raises(ValueError, match="eta_out"):
+        S.Sweep.run(sweep, eta_out=np.zeros(2))
+    with pytest.raises(ValueError, match="sh_out_all"):
+        S.Sweep.run(sweep, eta_out=np.zeros(3), sh_out_all=np.zeros(11, np.complex64))
+    with pytest.raises(ValueError, match="with_fields"):
+        S.Sweep.run(sweep, with_fields=True, sh_out_all=12345)
+    solve = types.SimpleNamespace(nx=8, ny=8)
+    with pytest.raises(ValueError, match="pump: 48 points"):
+        S.Solver.set_input_fields(solve, np.zeros((6, 8), np.complex64))
+    with pytest.raises(ValueError, match="sh: 72 points"):
+        S.Solver.set_input_fields(solve, np.zeros((8, 8), np.complex64), np.zeros((9, 8), np.complex64))
