@@ -69,9 +69,11 @@ def test_cli_runs_with_reference_argv(tmp_path):
     g = golden("stock_cli.npz")
     exe = os.path.join(ROOT, "shg_focused_gaussian_beams_gb300", "_build", "shg")
     r = subprocess.run([exe, "30", "29", "55.66", "55.66", "1", "0", "--outdir", str(tmp_path)], capture_output=True,
-                       text=True, timeout=300)
+                       text=True, timeout=300, cwd=str(tmp_path))
     assert r.returncode == 0, r.stderr
-    assert "Conversion efficiency" in r.stdout
+    assert "Conversion efficiency" in r.stdout and "Nonlinear crystal = MgO:sPPLT" in r.stdout
+    # SHG.cpp:85-97: the elapsed seconds appended to the per-grid timing file in the working directory
+    assert float(open(tmp_path / "CPUTime_NZ_200_N_64_T.txt").read().split()[-1]) > 0
     so = load_matrix_complex(str(tmp_path), "Signal_out")
     assert rel_l2(so, g["sh_out"]) < FIELD_RTOL
 
