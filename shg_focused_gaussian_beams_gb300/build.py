@@ -99,11 +99,12 @@ def build(force: bool = False, jobs: int = 8, verbose: bool = False, variant: st
             sys.stderr.write(err)
     objs = [_obj(s, v["out"]) for s in srcs]
     tmp = lib + f".tmp{os.getpid()}"
-    subprocess.run([NVCC] + ARCH + v["link"] + ["-shared", "-o", tmp] + objs + ["-lcudart"], check=True)
+    subprocess.run([NVCC] + ARCH + v["link"] + ["-shared", "-o", tmp] + objs + ["-lcudart", "-ldl"], check=True)
     os.replace(tmp, lib)
     if variant == "":
         tmp = CLI + f".tmp{os.getpid()}"
-        subprocess.run([NVCC] + ARCH + ["-o", tmp, _obj(os.path.join(CSRC, "shg_cli.cpp"))] + objs, check=True)
+        subprocess.run([NVCC] + ARCH + ["-o", tmp, _obj(os.path.join(CSRC, "shg_cli.cpp"))] + objs + ["-ldl"],
+                       check=True)
         os.replace(tmp, CLI)
     return lib
 

@@ -439,6 +439,7 @@ void shg_thgrad_destroy(shg_thgrad *h) { delete h; }
 
 int shg_thgrad_solve_temperature(shg_thgrad *h, int i, float power, float waist, float focal, float temp,
                                  float t_inf, float t1, float t2, int *counts) {
+    shg::Phase phase("shg_thgrad_solve_temperature");
     if (!h) return SHG_ERR_INVALID;
     return h->b.solve_temperature(i, power, waist, focal, temp, t_inf, t1, t2, counts);
 }
@@ -460,6 +461,7 @@ int shg_thgrad_gaussian_pumps(shg_thgrad *h, void *pump, void *stream) {
 
 int shg_thgrad_forward(shg_thgrad *h, const void *pump_in, void *pump_out, void *sh_out, double *p_sh, double *p_in,
                        void *stream) {
+    shg::Phase phase("shg_thgrad_forward");
     if (!h) return SHG_ERR_INVALID;
     return h->b.forward(static_cast<const float2 *>(pump_in), static_cast<float2 *>(pump_out),
                         static_cast<float2 *>(sh_out), p_sh, p_in, static_cast<cudaStream_t>(stream));
@@ -467,6 +469,7 @@ int shg_thgrad_forward(shg_thgrad *h, const void *pump_in, void *pump_out, void 
 
 int shg_thgrad_gradient(shg_thgrad *h, const void *pump_in, int checkpoints, void *grad_pump, double *p_sh,
                         double *p_in, void *stream) {
+    shg::Phase phase("shg_thgrad_gradient");
     if (!h) return SHG_ERR_INVALID;
     return h->b.gradient(static_cast<const float2 *>(pump_in), checkpoints, static_cast<float2 *>(grad_pump), p_sh,
                          p_in, static_cast<cudaStream_t>(stream));

@@ -1351,6 +1351,7 @@ int shg_set_input_fields(shg_handle *h, const float *pump, const float *sh) {
 }
 
 int shg_cwes(shg_handle *h, float temp) {
+    shg::Phase phase("shg_cwes");
     SHG_TRY(check_handle(h));
     if (h->th) {
         set_error("plain-path entry point called on a thermal handle");
@@ -1370,6 +1371,7 @@ int shg_cwes(shg_handle *h, float temp) {
 
 int shg_cwes_device(shg_handle *h, float temp, const void *pump_in, const void *sh_in, void *pump_out,
                     void *sh_out, void *stream) {
+    shg::Phase phase("shg_cwes_device");
     SHG_TRY(check_handle(h));
     if (h->th) {
         set_error("plain-path entry point called on a thermal handle");
@@ -1397,6 +1399,7 @@ int shg_cwes_device(shg_handle *h, float temp, const void *pump_in, const void *
 
 int shg_run(shg_handle *h, float power, float waist, float focalpoint, float temp, float t_inf, float t_peltier1,
             float t_peltier2, int save_only_last, int save_temperature) {
+    shg::Phase phase("shg_run");
     SHG_TRY(check_handle(h));
     (void)save_only_last;
     (void)save_temperature;
@@ -1484,6 +1487,7 @@ int shg_efficiency(shg_handle *h, double *eta) {
 
 int shg_grad_device(shg_handle *h, float temp, const void *pump_in, const void *sh_in, int checkpoints,
                     void *grad_pump, void *grad_sh, double *out4, void *stream) {
+    shg::Phase phase("shg_grad_device");
     SHG_TRY(check_handle(h));
     if (h->th) {
         set_error("shg_grad_device: gradients are for plain handles (hold the temperature field fixed)");
@@ -1512,6 +1516,7 @@ int shg_grad_device(shg_handle *h, float temp, const void *pump_in, const void *
 
 int shg_grad_run(shg_handle *h, float power, float waist, float focalpoint, float temp, const void *pump_factor,
                  int checkpoints, void *grad_pump, double *out8, void *stream) {
+    shg::Phase phase("shg_grad_run");
     SHG_TRY(check_handle(h));
     if (h->th) {
         set_error("shg_grad_run: gradients are for plain handles (hold the temperature field fixed)");
@@ -1660,6 +1665,7 @@ int shg_batch_destroy(shg_batch *b) {
 }
 
 int shg_batch_run_async(shg_batch *b, void *stream) {
+    shg::Phase phase("shg_batch_run_async");
     if (!b) {
         set_error("null batch");
         return SHG_ERR_INVALID;
@@ -1693,6 +1699,7 @@ int shg_batch_results(shg_batch *b, double *eta) {
 }
 
 int shg_batch_run(shg_batch *b, double *eta, float *sh_out_all) {
+    shg::Phase phase("shg_batch_run");
     if (!b) {
         set_error("null batch");
         return SHG_ERR_INVALID;
@@ -1799,6 +1806,7 @@ int shg_batch_launch_count(shg_batch *b, int *launches) {
 }
 
 int shg_batch_autotune(shg_batch *b, void *stream) {
+    shg::Phase phase("shg_batch_autotune");
     if (!b) {
         set_error("null argument");
         return SHG_ERR_INVALID;

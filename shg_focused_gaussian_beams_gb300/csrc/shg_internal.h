@@ -2,12 +2,23 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <string>
 
 #include "../../include/shg.h"
 
 namespace shg {
+
+// A named NVTX range over one host-side phase of an entry point (shown by Nsight tools and
+// usable as an ncu --nvtx filter); without an attached tool a push or pop is one test of a
+// function pointer.
+struct Phase {
+    explicit Phase(const char *name) { nvtxRangePushA(name); }
+    ~Phase() { nvtxRangePop(); }
+    Phase(const Phase &) = delete;
+    Phase &operator=(const Phase &) = delete;
+};
 
 struct InstDesc;
 

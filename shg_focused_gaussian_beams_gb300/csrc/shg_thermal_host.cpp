@@ -226,6 +226,7 @@ int ThermalSolve::sweeps_checked(float t_inf, int n) {
 // error word is read at every residual check, so a sweep whose pipeline gave up ends the
 // solve there (its stale voxels could otherwise keep the residual above the tolerance).
 int ThermalSolve::jacobi(float t_inf, int *counter) {
+    shg::Phase phase("Jacobi solve");
     const int rc = jacobi_run(t_inf, counter);
     if (rc) return rc;
     return heat_pipeline_ok(err_, st_);
@@ -308,6 +309,7 @@ int ThermalSolve::load_temperature(const float *T_host) {
 }
 
 int ThermalSolve::cwes(float power, float waist, float focal) {
+    shg::Phase phase("THERMAL CWES");
     const size_t nn = (size_t)n_ * n_;
     TH_TRY(tables());
     SolveParams sp{n_, nz_, cfg_.lx, cfg_.ly, power, waist, focal, tc_, tc_, tc_};
