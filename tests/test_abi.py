@@ -168,3 +168,31 @@ def test_binding_signatures_match_the_header_prototypes():
             continue
         bad += [(name, i, p) for i, (p, a) in enumerate(zip(params, args)) if not ok(p, a)]
     assert not bad, bad
+
+
+def test_argument_errors_are_reported_before_any_device_call():
+    """Grids the device path does not take, unknown crystals, empty batches and null
+    arguments return their status codes and messages from host checks alone (this runs
+    without a GPU)."""
+    import ctypes as C
+    from shg_focused_gaussian_beams_gb300 import _lib
+    L = _lib.lib()
+    h = C.c_void_p()
+    for over, code, msg in [(dict(nx=48, ny=48), 2, b"power of two"), (dict(nx=64, ny=32), 2, b"square grid"),
+                            (dict(nx=512, ny=512), 2, b"[16, 256]"), (dict(nz=1), 1, b"grid sizes")]:
+        cfg = _lib.default_config(**over)
+        assert L.shg_create(C.byref(cfg), C.byref(h)) == code and msg in L.shg_last_error(), over
+    n = C.c_float()
+    assert L.shg_index(7, 1.064, 50.0, C.byref(n)) == 1 and b"unknown crystal" in L.shg_last_error()
+    assert L.shg_index(0, -1.0, 50.0, C.byref(n)) == 1
+    assert L.shg_index(1, 1.064, 50.0, C.byref(n)) == 0 and 2.1 < n.value < 2.2
+    cfg = _lib.default_config()
+    assert L.shg_batch_create(C.byref(cfg), None, 0, C.byref(h)) == 1 and b"empty batch" in L.shg_last_error()
+    assert L.shg_thgrad_create(C.byref(cfg), 0, C.byref(h)) == 2 and b"count" in L.shg_last_error()
+    assert L.shg_dft2d_device(48, -1, None, None, None) == 1
+    assert L.shg_dft2d_device(64, 0, None, None, None) == 1
+    assert L.shg_run(None, 1, 1, 1, 1, 1, 1, 1, 1, 0) == 1 and b"null handle" in L.shg_last_error()
+    assert L.shg_cwes_noalloc(None, 50.0, None, None, None, None, None, None) == 1
+    assert L.shg_init_temperature(None, 50, 50, 50, 0, None) == 1 and b"null config" in L.shg_last_error()
+    assert L.shg_heat_sweeps(None, None, None, 25.0, 1, 0) == 1 and b"null config" in L.shg_last_error()
+    assert L.shg_destroy(None) == 0 and L.shg_batch_destroy(None) == 0
