@@ -58,3 +58,21 @@ def test_integration_snippet_compiles(k, tmp_path):
     r = subprocess.run([cxx, "-std=c++17", "-fsyntax-only", "-Wno-unused", "-I", os.path.join(ROOT, "include"),
                         str(src)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr + "\n" + src.read_text()
+
+
+def test_ctypes_stub_matches_the_binding(monkeypatch):
+    """The ctypes stub of the integration notes declares shg_config field for field like the
+    packaged binding, and its shg_config_init call fills the reference defaults (run up to
+    that call: the rest needs a GPU)."""
+    from shg_focused_gaussian_beams_gb300 import _lib
+    if not os.path.isfile(_lib.LIB_PATH):
+        pytest.skip("library not built")
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    stub = re.search(r"```python\n(.*?)```", text, flags=re.S).group(1)
+    stub = stub.split("h = C.c_void_p()")[0]
+    monkeypatch.chdir(ROOT)  # the stub loads the library by its path in the checkout
+    ns = {}
+    exec(compile(stub, "INTEGRATION.md", "exec"), ns)
+    assert ns["shg_config"]._fields_ == _lib.Config._fields_
+    cfg = ns["cfg"]
+    assert (cfg.nx, cfg.ny, cfg.nz, cfg.lz, cfg.crystal) == (64, 64, 200, 30000.0, 0)
