@@ -85,3 +85,20 @@ def test_weak_scaling_ranks_get_distinct_sweeps():
     a = rank_sweep(8, 5, 0, 2)
     b = rank_sweep(8, 5, 1, 2)
     assert len(a) == len(b) == 8 and [i.power for i in a] != [i.power for i in b]
+
+
+def test_partition_and_gather_edge_cases():
+    """More ranks than solves leaves ranks empty (nothing duplicated); an empty sweep gives
+    empty parts; on one process the gather returns the sweep order and refuses indices that
+    do not cover the sweep."""
+    import pytest
+    from shg_focused_gaussian_beams_gb300.parallel import gather_sweep
+    insts = W.config_sweep(count=3, seed=9)
+    parts = partition_lpt(insts, 5)
+    assert sorted(i for p in parts for i in p) == [0, 1, 2] and sum(1 for p in parts if not p) == 2
+    assert partition_lpt([], 3) == [[], [], []]
+    eta, f = gather_sweep([2, 0, 1], [0.3, 0.1, 0.2], 3, fields=["c", "a", "b"])
+    assert eta == [0.1, 0.2, 0.3] and f == ["a", "b", "c"]
+    assert gather_sweep([1, 0], [0.2, 0.1], 2) == ([0.1, 0.2], None)
+    with pytest.raises(ValueError, match="do not cover"):
+        gather_sweep([0, 2], [0.1, 0.3], 3)
