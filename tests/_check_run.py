@@ -201,6 +201,16 @@ def host_cases():
     record("index", same)
     record("index_bad_crystal", L.shg_index(7, 1.064, 50.0, C.byref(v)) != 0)
     record("null_args", L.shg_config_init(None) == 1 and L.shg_batch_create(None, None, 0, None) == 1)
+    h = C.c_void_p()
+    grids = [dict(nx=48, ny=48), dict(nx=64, ny=32), dict(nx=512, ny=512), dict(nz=1)]
+    record("unsupported_grids", all(L.shg_create(C.byref(_lib.default_config(**g)), C.byref(h)) in (1, 2)
+                                    and len(L.shg_last_error()) > 0 for g in grids))
+    cfg = _lib.default_config()
+    record("empty_batches", L.shg_batch_create(C.byref(cfg), None, 0, C.byref(h)) == 1
+           and L.shg_thgrad_create(C.byref(cfg), 0, C.byref(h)) == 2)
+    record("bad_dft_and_handles", L.shg_dft2d_device(48, -1, None, None, None) == 1
+           and L.shg_run(None, 1, 1, 1, 1, 1, 1, 1, 1, 0) == 1 and L.shg_destroy(None) == 0
+           and L.shg_batch_destroy(None) == 0 and L.shg_heat_sweeps(None, None, None, 25.0, 1, 0) == 1)
     e, s_, val = C.c_int(), C.c_int(), C.c_longlong()
     record("check_status", L.shg_check_status(C.byref(e), C.byref(s_), C.byref(val)) == 0 and e.value == 0)
 
