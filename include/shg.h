@@ -82,19 +82,24 @@ int shg_set_output_dir(shg_handle *h, const char *dir);
 /* Efields::setInputPump (Efields.h:174 -> setPump, Efields.h:74): Gaussian pump with the
  * refractive index taken at temperature tc. */
 int shg_set_input_pump(shg_handle *h, float power, float focalpoint, float waist, float tc);
-/* Arbitrary input fields (host, NX*NY complex each); sh may be NULL for a zero start. */
+/* Arbitrary input fields (host, NX*NY complex each); sh may be NULL for a zero start. The
+ * reference builds only the Gaussian of Efields.h:74-104 and the noise of Efields.h:129-144. */
 int shg_set_input_fields(shg_handle *h, const float *pump, const float *sh);
 /* Solver::CWES (Solver.h:245) without THERMAL from the current input fields, with the
  * propagators (Efields.h:186) and the constant phase mismatch (PhaseMatching.h:113)
  * set at temperature `temp`. */
 int shg_cwes(shg_handle *h, float temp);
-/* Same, with device pointers (NX*NY complex64 each) and a cudaStream_t (NULL = default). */
+/* Solver::CWES (Solver.h:245) as above, with device pointers (NX*NY complex64 each) and a
+ * cudaStream_t (NULL = default). */
 int shg_cwes_device(shg_handle *h, float temp, const void *pump_in, const void *sh_in, void *pump_out,
                     void *sh_out, void *stream);
 
-/* Results of the last run. Fields: host buffers of NX*NY complex (interleaved float). */
+/* Results of the last run: the Pump_out / Signal_out state of Solver.h:250-255. Fields: host
+ * buffers of NX*NY complex (interleaved float). */
 int shg_get_fields(shg_handle *h, float *pump_out, float *sh_out);
-/* P = 1/2 eps0 c n sum|A|^2 dx dy with n the pump / SH index at the run temperature. */
+/* P = 1/2 eps0 c n sum|A|^2 dx dy with n the pump / SH index at the run temperature, and the
+ * efficiency P_SH(out) / P_pump(in) (the reference prints neither; its power normalisation
+ * is that of setPump, Efields.h:88). */
 int shg_get_powers(shg_handle *h, double *p_pump_in, double *p_sh_out, double *p_pump_out);
 int shg_efficiency(shg_handle *h, double *eta);
 
@@ -145,13 +150,14 @@ int shg_get_jacobi_residual(shg_handle *h, double *rel);
 int shg_init_temperature(const shg_config *cfg, float temp, float t1, float t2, int bc, float *T_out);
 int shg_heat_sweeps(const shg_config *cfg, float *T_inout, const float *Q, float t_inf, int nsweeps, int bc);
 int shg_dk_thermal(const shg_config *cfg, const float *T, float *DK, float *NP, float *NS);
-/* `nsweeps` heat sweeps on device buffers: Ta holds T on entry, Tb an identical copy (the
+/* `nsweeps` heat sweeps (Tfield.h:113 / Tfield.h:224) on device buffers: Ta holds T on entry, Tb an identical copy (the
  * voxels the stencil never writes must match); sweep k writes the other buffer, so the
  * result is in Ta for even nsweeps and in Tb for odd. QK = Q / k_th per voxel. */
 int shg_heat_sweeps_device(const shg_config *cfg, void *Ta, void *Tb, const void *QK, float t_inf, int nsweeps, int bc,
                            void *stream);
 
 /* ---- Batched sweep: many independent plain solves in one device schedule ----------- */
+/* Replaces SHG.sh:73-101, which runs one ./SHG process per sweep point (SHG.sh:81). */
 typedef struct shg_instance {
     int nx, ny, nz;          /* per-solve grid (square, power of two) */
     float lx, ly;            /* per-solve window */
@@ -299,7 +305,7 @@ double shg_thgrad_device_bytes(const shg_thgrad *b);
 
 /* ---- Components, for tests ------------------------------------------------------- */
 /* Unnormalised 2D DFT of an n x n complex array on the device (sign -1 forward, +1
- * backward, FFTW's convention), device pointers, in place allowed. */
+ * backward, FFTW's convention; the fftwf plans of Solver::diffraction, Solver.h:156-190), device pointers, in place allowed. */
 int shg_dft2d_device(int n, int sign, const void *in, void *out, void *stream);
 
 #ifdef __cplusplus
